@@ -1,0 +1,368 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 droplet step: prints ONE JSON line.
+
+A "step" is one time step of the D3Q15 two-phase droplet update over the
+whole resident domain. The default workload is the forced-turbulence case
+(128^3, LES, constant-injection band forcing, one droplet R = 16), run in the
+FP32 form; --form and --workload select others.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the CPU implementation of the same step on the host
+cores (the oracle's OpenMP restatement of the reference, which cannot itself
+be built here: it is Fortran + MPI + 2decomp_fft). Under torchrun only rank 0
+runs it. The path has no exchange step between independent droplet domains,
+so N > 1 runs N independent replicas ("replicas only"), weak scaling.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "MLUPS and % HBM roofline, chosen vs plain FP64 form at stated φ error; adjoint/fwd"
+UNIT = "MLUPS"
+# algorithmic bytes per lattice update: 2 distributions x 15 x (read + write) x bytes per population
+BYTES_PER_SITE = {64: 480, 32: 240, 16: 120}
+FORMS = {"fp64": 64, "fp32": 32, "fp16": 16}
+DTYPE = {64: "f64", 32: "f32", 16: "f32 (f16 storage)"}
+MAIN_KERNEL = {64: "collide_fp64", 32: "step_fused", 16: "step_fused"}
+
+
+def measured_peak_gbs():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def committed_traffic(kernel: str, workload: str):
+    """DRAM bytes per launch from the committed ncu summary, if one exists."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(p) as fh:
+            d = json.load(fh)
+        return d.get(f"{kernel}:{workload}")
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.dev = device_index
+        self.proc = None
+        self.path = os.path.join("/tmp", f"dl_clocks_{os.getpid()}.csv")
+
+    def start(self):
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        sm, smax, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        with open(self.path) as fh:
+            for line in fh:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    smax.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for n, v in zip(names, parts[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(n)
+        try:
+            os.remove(self.path)
+        except OSError:
+            pass
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_workload(name: str, form: int):
+    from droplet_gb300 import configs
+
+    if name == "config1":
+        w = configs.config1()
+        w.form = form
+    elif name == "config2":
+        w = configs.config2(form=form)
+    elif name == "config3":
+        w = configs.config3()
+        w.form = form
+    else:
+        raise SystemExit(f"unknown workload {name}")
+    return w
+
+
+def new_sim(w, rank: int = 0):
+    from droplet_gb300.solver import Droplet
+
+    sim = Droplet(w.params, w.shape, w.form)
+    sim.set_fields(**w.fields)
+    sim.init_equilibrium()
+    sim.set_force(w.force_mode)
+    return sim
+
+
+def cpu_baseline(w, budget_s: float = 15.0, threads: int | None = None):
+    """Oracle (OpenMP restatement) MLUPS on this host on a bounded sample of
+    the workload: the full domain when a step fits the budget, else a slab."""
+    from oracle import pyoracle
+
+    threads = threads or os.cpu_count() or 1
+    pyoracle.set_threads(threads)
+    nx, ny, nz = w.shape
+    o = pyoracle.OracleDroplet(w.params, w.shape)
+    o.set_fields(**w.fields)
+    o.init_equilibrium()
+    o.set_force(w.force_mode)
+    t0 = time.perf_counter()
+    o.step(1)
+    t1 = time.perf_counter()
+    per = t1 - t0
+    steps = max(1, min(200, int(budget_s / max(per, 1e-6))))
+    t0 = time.perf_counter()
+    o.step(steps)
+    dt = time.perf_counter() - t0
+    o.close()
+    return {"value": round(nx * ny * nz * steps / dt / 1e6, 3), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{steps} steps of the full {nx}x{ny}x{nz} workload after 1 warm-up step, "
+                      f"FP64 C/OpenMP restatement of the reference loops ({threads} threads)"}
+
+
+def run_reference(args):
+    """--impl reference: the CPU restatement on all host cores, K timed steps
+    on a slab of the workload sized to keep the run within a few minutes."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    import numpy as np
+    from oracle import pyoracle
+    from droplet_gb300 import configs
+
+    form = FORMS[args.form]
+    w = make_workload(args.workload, form)
+    threads = os.cpu_count() or 1
+    pyoracle.set_threads(threads)
+    nx, ny, nz = w.shape
+    # probe the per-site rate on one step of the full domain
+    o = pyoracle.OracleDroplet(w.params, w.shape)
+    o.set_fields(**w.fields)
+    o.init_equilibrium()
+    o.set_force(w.force_mode)
+    t0 = time.perf_counter()
+    o.step(1)
+    rate = nx * ny * nz / (time.perf_counter() - t0)
+    o.close()
+    budget = 120.0
+    total_steps = args.steps + args.warmup
+    nz_s = int(max(8, min(nz, budget * rate / (nx * ny * max(total_steps, 1)))))
+    sub = dict((k, np.ascontiguousarray(v[:nz_s])) for k, v in w.fields.items())
+    P = w.params
+    o = pyoracle.OracleDroplet(P, (nx, ny, nz_s))
+    o.set_fields(**sub)
+    o.init_equilibrium()
+    o.set_force(w.force_mode)
+    o.step(args.warmup)
+    t0 = time.perf_counter()
+    o.step(args.steps)
+    dt = time.perf_counter() - t0
+    sites = nx * ny * nz_s
+    value = sites * args.steps / dt / 1e6
+    sample = (f"{args.steps} timed steps (after {args.warmup} warm-up) of a {nx}x{ny}x{nz_s} slab of the "
+              f"{w.name} workload, same physics; FP64 C/OpenMP restatement of the reference loops")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt * 1e3 / max(args.steps, 1), 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded)",
+        "config": {"workload": w.name, "form": "fp64 (CPU)", "sites": sites, "seed": w.seed},
+        "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    form = FORMS[args.form]
+    w = make_workload(args.workload, form)
+    nx, ny, nz = w.shape
+    N = nx * ny * nz
+    stream = torch.cuda.Stream()
+    sim = new_sim(w, rank)
+    sim.set_stream(stream.cuda_stream)
+    sim.step(args.warmup)
+    sim.sync()
+
+    # ---- timed region: K steps, events on the library's stream -------------------
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    time.sleep(0.3)
+    sim.profile(True)
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    sim.step(args.steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    ms = e0.elapsed_time(e1)
+    prof = sim.profile_read()
+    sim.profile(False)
+    clk = clocks.stop()
+    sim.sync()  # raises if the NaN watchdog tripped
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = N * args.steps * world / (ms / 1e3) / 1e6
+
+    # roofline of the dominant kernel (live per-launch events over the timed region)
+    peak, peak_kind = measured_peak_gbs()
+    avg_main_ms = prof["main_ms"] / max(prof["main_launches"], 1)
+    bytes_per_launch = BYTES_PER_SITE[form] * N
+    achieved = bytes_per_launch / (avg_main_ms / 1e3) / 1e9
+    traffic = committed_traffic(MAIN_KERNEL[form], w.name)
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_kind,
+                "kernel": MAIN_KERNEL[form], "kernel_ms": round(avg_main_ms, 5),
+                "kernel_share": round(prof["main_ms"] / max(prof["total_ms"], 1e-12), 4),
+                "algorithmic_bytes_per_launch": bytes_per_launch}
+
+    # ---- e2e through the C-ABI with host buffers ------------------------------------
+    e2e = None
+    if not args.no_e2e:
+        k_e2e = min(args.steps, 500)
+        pinned = {k: torch.from_numpy(np.ascontiguousarray(v)).pin_memory().numpy() for k, v in w.fields.items()}
+        out = {k: torch.empty(v.shape, dtype=torch.float64).pin_memory().numpy() for k, v in w.fields.items()}
+        from droplet_gb300.solver import Droplet
+
+        sim2 = Droplet(w.params, w.shape, w.form)
+        sim2.set_stream(stream.cuda_stream)
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+        t0 = time.perf_counter()
+        sim2.set_fields(**pinned)
+        sim2.init_equilibrium()
+        sim2.set_force(w.force_mode)
+        for _ in range(k_e2e):
+            sim2.step(1)
+            sim2.reduce()  # device -> host read of the step's diagnostics
+        sim2.get_fields_into(out)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        if dist is not None:
+            t = torch.tensor([dt], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            dt = float(t.item())
+        sim2.close()
+        from droplet_gb300 import _abi
+        import ctypes
+
+        h2d = 5 * N * 8
+        d2h = 5 * N * 8 + k_e2e * ctypes.sizeof(_abi.DLDiag)
+        e2e = {"value": round(N * k_e2e * world / dt / 1e6, 3), "unit": UNIT,
+               "h2d_bytes_per_step": int(round(h2d / k_e2e)), "d2h_bytes_per_step": int(round(d2h / k_e2e)),
+               "steps": k_e2e,
+               "note": "set_fields(host) + init_equilibrium + per step: dl_step(1) and dl_reduce (D2H of the "
+                       "diagnostics) + final dl_get_fields(host), all timed"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(w, budget_s=args.cpu_budget)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 5), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": DTYPE[form], "data": "synthetic (seeded)",
+            "config": {"workload": w.name, "form": args.form, "sites": N, "shape": list(w.shape),
+                       "seed": w.seed, "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                       "l2": "inputs larger than L2 (populations {:.0f} MB)".format(
+                           2 * 15 * N * BYTES_PER_SITE[form] / 60 / 1e6),
+                       "notes": w.notes},
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "clocks": clk,
+            "gpu_launches": int(prof["launches"]),
+        }
+        print(json.dumps(line), flush=True)
+    sim.close()
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--form", choices=sorted(FORMS), default="fp64")
+    ap.add_argument("--workload", default="config2")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

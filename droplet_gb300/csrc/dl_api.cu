@@ -1,0 +1,368 @@
+// dl_api.cu -- the extern "C" entry points of include/droplet_gb300.h.
+// Host-side handle management, argument checking, host<->device layout
+// conversion and dispatch to the form-specific kernels.
+#include "dl_internal.cuh"
+
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <new>
+
+namespace dl {
+
+int set_error(dl_handle* h, int code, const char* fmt, ...) {
+    if (h) {
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(h->err, sizeof(h->err), fmt, ap);
+        va_end(ap);
+    }
+    return code;
+}
+
+int check_cuda(dl_handle* h, cudaError_t e, const char* what) {
+    return set_error(h, DL_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+void launch_begin(dl_handle* h) {
+    if (!h->prof_on) return;
+    if (h->prof_n == h->prof_cap) {
+        int cap = h->prof_cap ? 2 * h->prof_cap : 256;
+        void* p = realloc(h->prof, sizeof(dl_handle::ProfEv) * cap);
+        if (!p) {
+            h->prof_on = 0;
+            return;
+        }
+        h->prof = (dl_handle::ProfEv*)p;
+        for (int k = h->prof_cap; k < cap; ++k) {
+            cudaEventCreate(&h->prof[k].a);
+            cudaEventCreate(&h->prof[k].b);
+        }
+        h->prof_cap = cap;
+    }
+    cudaEventRecord(h->prof[h->prof_n].a, h->stream);
+}
+
+void launch_end(dl_handle* h, bool main_kernel) {
+    h->launches += 1;
+    if (!h->prof_on) return;
+    cudaEventRecord(h->prof[h->prof_n].b, h->stream);
+    h->prof[h->prof_n].main = main_kernel ? 1 : 0;
+    h->prof_n += 1;
+}
+
+static void prof_release(dl_handle* h) {
+    for (int k = 0; k < h->prof_cap; ++k) {
+        cudaEventDestroy(h->prof[k].a);
+        cudaEventDestroy(h->prof[k].b);
+    }
+    free(h->prof);
+    h->prof = nullptr;
+    h->prof_cap = h->prof_n = 0;
+}
+
+static void init_consts(dl_handle* h) {
+    // program/lbm_drop_xy.f90:77-84, each entry rounded as the reference rounds it
+    const double E[Q] = {2.0 / 9.0,  1.0 / 9.0,  1.0 / 9.0,  1.0 / 9.0,  1.0 / 9.0,
+                         1.0 / 9.0,  1.0 / 9.0,  1.0 / 72.0, 1.0 / 72.0, 1.0 / 72.0,
+                         1.0 / 72.0, 1.0 / 72.0, 1.0 / 72.0, 1.0 / 72.0, 1.0 / 72.0};
+    const double F[Q] = {-7.0 / 3.0, 1.0 / 3.0,  1.0 / 3.0,  1.0 / 3.0,  1.0 / 3.0,
+                         1.0 / 3.0,  1.0 / 3.0,  1.0 / 24.0, 1.0 / 24.0, 1.0 / 24.0,
+                         1.0 / 24.0, 1.0 / 24.0, 1.0 / 24.0, 1.0 / 24.0, 1.0 / 24.0};
+    for (int i = 0; i < Q; ++i) {
+        h->lc.E[i] = E[i];
+        h->lc.F[i] = F[i];
+        h->lc.Ekf[i] = E[i] * h->P.kappaf;
+        h->lc.Ekg[i] = E[i] * h->P.kappag;
+        h->lc.ds3E[i] = (3.0 * h->P.ds) * E[i];
+        h->lc.six_E[i] = 6.0 * E[i];
+    }
+}
+
+static int reset_state(dl_handle* h) {
+    DevState s;
+    memset(&s, 0, sizeof(s));
+    s.phi_min = h->P.phi1;
+    s.phi_max = h->P.phi2;
+    s.key_min = KEY_POS_INF;
+    s.key_max = KEY_NEG_INF;
+    DL_CUDA(h, cudaMemcpyAsync(h->d_state, &s, sizeof(s), cudaMemcpyHostToDevice, h->stream));
+    DL_CUDA(h, cudaStreamSynchronize(h->stream));
+    return DL_OK;
+}
+
+static int set_minmax(dl_handle* h, double mn, double mx) {
+    double v[2] = {mn, mx};
+    DL_CUDA(h, cudaMemcpyAsync(h->d_state, v, sizeof(v), cudaMemcpyHostToDevice, h->stream));
+    DL_CUDA(h, cudaStreamSynchronize(h->stream));
+    return DL_OK;
+}
+
+// Device scratch for a host<->device transfer of one SoA array set.
+struct Staging {
+    double* d = nullptr;
+    ~Staging() {
+        if (d) cudaFree(d);
+    }
+};
+
+}  // namespace dl
+
+using namespace dl;
+
+extern "C" {
+
+int dl_version(void) { return 100; }
+
+const char* dl_status_string(int status) {
+    switch (status) {
+        case DL_OK: return "ok";
+        case DL_ERR_ARG: return "bad argument";
+        case DL_ERR_CUDA: return "CUDA error";
+        case DL_ERR_ALLOC: return "allocation failed";
+        case DL_ERR_NAN: return "NaN/Inf detected";
+        case DL_ERR_TIMEOUT: return "device wait timed out";
+        case DL_ERR_STATE: return "call out of order";
+        case DL_ERR_UNSUPPORTED: return "unsupported option for this form";
+        default: return "unknown status";
+    }
+}
+
+int dl_create(const dl_params* params, int nx, int ny, int nz, int form, dl_handle** out) {
+    if (!params || !out) return DL_ERR_ARG;
+    *out = nullptr;
+    if (nx < 3 || ny < 3 || nz < 3) return DL_ERR_ARG;
+    if (form != DL_FORM_FP64) return DL_ERR_UNSUPPORTED;
+    if (params->tauf <= 0.5 || params->ds <= 0.0 || params->phi2 == params->phi1) return DL_ERR_ARG;
+    if (params->kc < 0 || params->visc_mode < 0 || params->visc_mode > 1) return DL_ERR_ARG;
+    dl_handle* h = new (std::nothrow) dl_handle();
+    if (!h) return DL_ERR_ALLOC;
+    memset(h, 0, sizeof(*h));
+    h->P = *params;
+    h->nx = nx;
+    h->ny = ny;
+    h->nz = nz;
+    h->N = (size_t)nx * ny * nz;
+    h->form = form;
+    h->stream = 0;
+    h->force_mode = DL_FORCE_NONE;
+    cudaError_t e = cudaGetDevice(&h->device);
+    if (e != cudaSuccess) {
+        delete h;
+        return DL_ERR_CUDA;
+    }
+    init_consts(h);
+    int rc = DL_OK;
+    if (cudaMalloc(&h->d_state, sizeof(DevState)) != cudaSuccess) rc = DL_ERR_ALLOC;
+    if (rc == DL_OK) rc = reset_state(h);
+    if (rc == DL_OK) rc = fp64_alloc(h);
+    if (rc == DL_OK) rc = spectral_alloc(h);
+    if (rc != DL_OK) {
+        dl_destroy(h);
+        return rc == DL_ERR_CUDA ? DL_ERR_ALLOC : rc;
+    }
+    *out = h;
+    return DL_OK;
+}
+
+int dl_destroy(dl_handle* h) {
+    if (!h) return DL_ERR_ARG;
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    fp64_free(h);
+    spectral_free(h);
+    cudaFree(h->d_state);
+    cudaFree(h->d_diag);
+    prof_release(h);
+    delete h;
+    return DL_OK;
+}
+
+int dl_profile(dl_handle* h, int enable) {
+    if (!h) return DL_ERR_ARG;
+    DL_CUDA(h, cudaStreamSynchronize(h->stream));
+    h->prof_on = enable ? 1 : 0;
+    h->prof_n = 0;
+    h->launches = 0;
+    return DL_OK;
+}
+
+int dl_profile_read(dl_handle* h, dl_profile_stats* out) {
+    if (!h || !out) return DL_ERR_ARG;
+    DL_CUDA(h, cudaStreamSynchronize(h->stream));
+    memset(out, 0, sizeof(*out));
+    for (int k = 0; k < h->prof_n; ++k) {
+        float ms = 0.f;
+        DL_CUDA(h, cudaEventElapsedTime(&ms, h->prof[k].a, h->prof[k].b));
+        out->total_ms += ms;
+        out->timed_launches += 1;
+        if (h->prof[k].main) {
+            out->main_ms += ms;
+            out->main_launches += 1;
+        }
+    }
+    out->launches = h->launches;
+    h->prof_n = 0;
+    h->launches = 0;
+    return DL_OK;
+}
+
+int dl_set_stream(dl_handle* h, void* stream) {
+    if (!h) return DL_ERR_ARG;
+    h->stream = (cudaStream_t)stream;
+    return DL_OK;
+}
+
+int dl_set_fields(dl_handle* h, const double* phi, const double* u1, const double* u2, const double* u3,
+                  const double* p) {
+    if (!h || !phi || !u1 || !u2 || !u3 || !p) return DL_ERR_ARG;
+    const size_t N = h->N;
+    double* d = h->mac64[h->cur];
+    const double* src[5] = {phi, u1, u2, u3, p};
+    for (int k = 0; k < 5; ++k)
+        DL_CUDA(h, cudaMemcpyAsync(d + k * N, src[k], N * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    DL_CUDA(h, cudaStreamSynchronize(h->stream));
+    h->fields_set = true;
+    return DL_OK;
+}
+
+int dl_get_fields(dl_handle* h, double* phi, double* u1, double* u2, double* u3, double* p) {
+    if (!h || !phi || !u1 || !u2 || !u3 || !p) return DL_ERR_ARG;
+    const size_t N = h->N;
+    const double* d = h->mac64[h->cur];
+    double* dst[5] = {phi, u1, u2, u3, p};
+    for (int k = 0; k < 5; ++k)
+        DL_CUDA(h, cudaMemcpyAsync(dst[k], d + k * N, N * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    DL_CUDA(h, cudaStreamSynchronize(h->stream));
+    return DL_OK;
+}
+
+int dl_init_equilibrium(dl_handle* h) {
+    if (!h) return DL_ERR_ARG;
+    if (!h->fields_set) return set_error(h, DL_ERR_STATE, "dl_init_equilibrium before dl_set_fields");
+    int rc = set_minmax(h, h->P.phi1, h->P.phi2);
+    if (rc != DL_OK) return rc;
+    rc = fp64_init_equilibrium(h);
+    if (rc != DL_OK) return rc;
+    DL_CUDA(h, cudaStreamSynchronize(h->stream));
+    h->eq_init = true;
+    return DL_OK;
+}
+
+int dl_set_force(dl_handle* h, int mode, const double* fx, const double* fy, const double* fz) {
+    if (!h) return DL_ERR_ARG;
+    const size_t N = h->N;
+    if (mode == DL_FORCE_STATIC) {
+        if (!fx || !fy || !fz) return DL_ERR_ARG;
+        const double* src[3] = {fx, fy, fz};
+        for (int k = 0; k < 3; ++k)
+            DL_CUDA(h, cudaMemcpyAsync(h->force64 + k * N, src[k], N * sizeof(double), cudaMemcpyHostToDevice,
+                                       h->stream));
+    } else if (mode == DL_FORCE_NONE || mode == DL_FORCE_SPECTRAL) {
+        if (mode == DL_FORCE_SPECTRAL && (h->P.kc < 2 || h->sp.K < 1))
+            return set_error(h, DL_ERR_ARG, "spectral forcing needs kc >= 2");
+        DL_CUDA(h, cudaMemsetAsync(h->force64, 0, 3 * N * sizeof(double), h->stream));
+    } else {
+        return DL_ERR_ARG;
+    }
+    DL_CUDA(h, cudaStreamSynchronize(h->stream));
+    h->force_mode = mode;
+    return DL_OK;
+}
+
+int dl_step(dl_handle* h, int nsteps) {
+    if (!h || nsteps < 0) return DL_ERR_ARG;
+    if (!h->eq_init) return set_error(h, DL_ERR_STATE, "dl_step before dl_init_equilibrium / dl_set_populations");
+    for (int k = 0; k < nsteps; ++k) {
+        int rc = fp64_step(h);
+        if (rc != DL_OK) return rc;
+    }
+    return DL_OK;
+}
+
+int dl_get_populations(dl_handle* h, double* f, double* g) {
+    if (!h || !f || !g) return DL_ERR_ARG;
+    const size_t bytes = Q * h->N * sizeof(double);
+    Staging st;
+    DL_CUDA(h, cudaMalloc(&st.d, bytes));
+    int rc = soa_to_aos(h, h->f64[h->cur], st.d);
+    if (rc != DL_OK) return rc;
+    DL_CUDA(h, cudaMemcpyAsync(f, st.d, bytes, cudaMemcpyDeviceToHost, h->stream));
+    DL_CUDA(h, cudaStreamSynchronize(h->stream));
+    rc = soa_to_aos(h, h->g64[h->cur], st.d);
+    if (rc != DL_OK) return rc;
+    DL_CUDA(h, cudaMemcpyAsync(g, st.d, bytes, cudaMemcpyDeviceToHost, h->stream));
+    DL_CUDA(h, cudaStreamSynchronize(h->stream));
+    return DL_OK;
+}
+
+int dl_set_populations(dl_handle* h, const double* f, const double* g) {
+    if (!h || !f || !g) return DL_ERR_ARG;
+    const size_t bytes = Q * h->N * sizeof(double);
+    Staging st;
+    DL_CUDA(h, cudaMalloc(&st.d, bytes));
+    DL_CUDA(h, cudaMemcpyAsync(st.d, f, bytes, cudaMemcpyHostToDevice, h->stream));
+    int rc = aos_to_soa(h, st.d, h->f64[h->cur]);
+    if (rc != DL_OK) return rc;
+    DL_CUDA(h, cudaStreamSynchronize(h->stream));
+    DL_CUDA(h, cudaMemcpyAsync(st.d, g, bytes, cudaMemcpyHostToDevice, h->stream));
+    rc = aos_to_soa(h, st.d, h->g64[h->cur]);
+    if (rc != DL_OK) return rc;
+    rc = fp64_moments_from_populations(h);
+    if (rc != DL_OK) return rc;
+    DL_CUDA(h, cudaStreamSynchronize(h->stream));
+    h->fields_set = true;
+    h->eq_init = true;
+    return DL_OK;
+}
+
+int dl_set_step(dl_handle* h, int64_t step) {
+    if (!h || step < 0) return DL_ERR_ARG;
+    h->step = step;
+    return DL_OK;
+}
+
+int dl_get_step(dl_handle* h, int64_t* step) {
+    if (!h || !step) return DL_ERR_ARG;
+    *step = h->step;
+    return DL_OK;
+}
+
+int dl_get_minmax(dl_handle* h, double* mn, double* mx) {
+    if (!h || !mn || !mx) return DL_ERR_ARG;
+    double v[2];
+    DL_CUDA(h, cudaMemcpyAsync(v, h->d_state, sizeof(v), cudaMemcpyDeviceToHost, h->stream));
+    DL_CUDA(h, cudaStreamSynchronize(h->stream));
+    *mn = v[0];
+    *mx = v[1];
+    return DL_OK;
+}
+
+int dl_sync(dl_handle* h) {
+    if (!h) return DL_ERR_ARG;
+    DL_CUDA(h, cudaStreamSynchronize(h->stream));
+    DevState s;
+    DL_CUDA(h, cudaMemcpy(&s, h->d_state, sizeof(s), cudaMemcpyDeviceToHost));
+    if (s.nan_flag) return set_error(h, DL_ERR_NAN, "non-finite phi/u/p first seen at step %lld", s.nan_step);
+    return DL_OK;
+}
+
+int dl_reduce(dl_handle* h, dl_diag* out) {
+    if (!h || !out) return DL_ERR_ARG;
+    int rc = reduce_fields(h, h->mac64[h->cur], out);
+    if (rc != DL_OK) return rc;
+    DevState s;
+    DL_CUDA(h, cudaMemcpy(&s, h->d_state, sizeof(s), cudaMemcpyDeviceToHost));
+    out->step = h->step;
+    out->nan_flag = s.nan_flag;
+    return DL_OK;
+}
+
+int dl_last_error(dl_handle* h, char* buf, int buflen) {
+    if (!h || !buf || buflen <= 0) return DL_ERR_ARG;
+    snprintf(buf, (size_t)buflen, "%s", h->err);
+    return DL_OK;
+}
+
+}  // extern "C"

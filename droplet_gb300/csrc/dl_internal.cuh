@@ -1,0 +1,173 @@
+// dl_internal.cuh -- internal declarations shared by the translation units of
+// libdroplet_gb300.so. Not part of the C-ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stddef.h>
+#include <string.h>
+
+#include "../../include/droplet_gb300.h"
+
+namespace dl {
+
+// D3Q15 lattice (program/lbm_drop_xy.f90:70-84); directions 0..14 = reference 1..15.
+constexpr int Q = 15;
+__host__ __device__ constexpr int cx(int i) {
+    return (i == 1 || i == 7 || i == 9 || i == 10 || i == 12) ? 1
+         : (i == 4 || i == 8 || i == 11 || i == 13 || i == 14) ? -1 : 0;
+}
+__host__ __device__ constexpr int cy(int i) {
+    return (i == 2 || i == 7 || i == 8 || i == 10 || i == 13) ? 1
+         : (i == 5 || i == 9 || i == 11 || i == 12 || i == 14) ? -1 : 0;
+}
+__host__ __device__ constexpr int cz(int i) {
+    return (i == 3 || i == 7 || i == 8 || i == 9 || i == 14) ? 1
+         : (i == 6 || i == 10 || i == 11 || i == 12 || i == 13) ? -1 : 0;
+}
+// weight class: 0 rest, 1 axis, 2 body diagonal
+__host__ __device__ constexpr int wclass(int i) { return i == 0 ? 0 : (i <= 6 ? 1 : 2); }
+
+// Host-computed constants (double), in the reference's rounding: each entry is
+// the correctly rounded value of the reference's constant expression.
+struct LatticeConsts {
+    double E[Q], F[Q];
+    double Ekf[Q];     // E(i)*kappaf
+    double Ekg[Q];     // E(i)*kappag
+    double ds3E[Q];    // (3*ds)*E(i)
+    double six_E[Q];   // 6*E(i)
+};
+
+// Device-resident per-handle state (scratch: reduction accumulators, flags).
+struct DevState {
+    double phi_min, phi_max;         // tau_g interpolation range of the next step
+    long long key_min, key_max;      // ordered-integer min/max accumulators of this step
+    unsigned int blocks_done;        // last-block ticket of the step kernel
+    int nan_flag;                    // nonzero once a non-finite value was produced
+    long long nan_step;              // step at which it was first seen
+    int quirk_scans;                 // number of exact serial-order min scans taken
+    int pad_;
+    // spectral forcing
+    double sp_energy;                // band energy of the last forcing evaluation
+    double sp_coef;                  // 0.5 eps / E
+};
+
+// Ordered mapping of a double to a signed 64-bit key (monotone for non-NaN).
+__host__ __device__ inline long long dbl_key(double v) {
+#ifdef __CUDA_ARCH__
+    long long b = __double_as_longlong(v);
+#else
+    long long b;
+    memcpy(&b, &v, 8);
+#endif
+    return b >= 0 ? b : (b ^ 0x7FFFFFFFFFFFFFFFLL);
+}
+__host__ __device__ inline double key_dbl(long long k) {
+    long long b = k >= 0 ? k : (k ^ 0x7FFFFFFFFFFFFFFFLL);
+#ifdef __CUDA_ARCH__
+    return __longlong_as_double(b);
+#else
+    double v;
+    memcpy(&v, &b, 8);
+    return v;
+#endif
+}
+constexpr long long KEY_POS_INF = 0x7FF0000000000000LL;                  // key of +inf
+constexpr long long KEY_NEG_INF = (long long)0xFFF0000000000000ULL ^ 0x7FFFFFFFFFFFFFFFLL;  // key of -inf
+
+// Spectral forcing tables (band 1 <= |k| < kc, half spectrum kz >= 0).
+struct SpectralPlan {
+    int K;            // kc - 1
+    int nmodes;       // number of half-spectrum band modes
+    double* d_twx;    // [nx][2] cos, sin of 2 pi m / nx
+    double* d_twy;    // [ny][2]
+    double* d_twz;    // [nz][2]
+    double* d_a1;     // [3][2K+1][ny*nz] complex   (x stage)
+    double* d_uh;     // [3][2K+1][2K+1][K+1] complex (band coefficients, /N)
+    double* d_b2;     // [3][2K+1][ny*nz] complex   (synthesis, x pending)
+};
+
+}  // namespace dl
+
+struct dl_handle {
+    dl_params P;
+    int nx, ny, nz;
+    size_t N;
+    int form;
+    int device;
+    cudaStream_t stream;
+    int cur;                 // index of the current population / field buffer
+    int64_t step;
+    int force_mode;
+    bool fields_set;
+    bool eq_init;
+    char err[512];
+
+    dl::LatticeConsts lc;
+    dl::DevState* d_state;   // device scratch
+
+    // FP64 form
+    double* f64[2];          // SoA populations [15][N], two buffers
+    double* g64[2];
+    double* mac64[2];        // [5][N]: phi, u1, u2, u3, p
+    double* rec64;           // derived records, [NREC][N]
+    int nrec;
+    double* force64;         // [3][N]
+
+    // reduced precision forms (FP32 / FP16 storage)
+    void* fs[2];             // populations, storage type of the form
+    void* gs[2];
+    float* mac32[2];         // [5][N]
+    double* force32_unused;
+
+    dl::SpectralPlan sp;
+    double* d_diag;          // diagnostics partial sums
+    int diag_blocks;
+
+    // launch accounting (dl_profile)
+    int64_t launches;
+    int prof_on;
+    struct ProfEv {
+        cudaEvent_t a, b;
+        int main;
+    } * prof;
+    int prof_n, prof_cap;
+};
+
+namespace dl {
+// fp64 form (step_fp64.cu)
+int fp64_alloc(dl_handle* h);
+void fp64_free(dl_handle* h);
+int fp64_init_equilibrium(dl_handle* h);
+int fp64_step(dl_handle* h);
+int fp64_moments_from_populations(dl_handle* h);
+// spectral forcing (spectral.cu)
+int spectral_alloc(dl_handle* h);
+void spectral_free(dl_handle* h);
+int spectral_force_fp64(dl_handle* h, const double* d_u1, const double* d_u2, const double* d_u3,
+                        double* d_fx, double* d_fy, double* d_fz);
+// transposes (layout.cu)
+int soa_to_aos(dl_handle* h, const double* d_soa, double* d_aos);
+int aos_to_soa(dl_handle* h, const double* d_aos, double* d_soa);
+// diagnostics (reduce.cu)
+int reduce_fields(dl_handle* h, const double* d_mac, dl_diag* out);
+
+int set_error(dl_handle* h, int code, const char* fmt, ...);
+// bracket one kernel launch: counts it and, when profiling, records events
+void launch_begin(dl_handle* h);
+void launch_end(dl_handle* h, bool main_kernel);
+int check_cuda(dl_handle* h, cudaError_t e, const char* what);
+}  // namespace dl
+
+#define DL_LAUNCH(h, is_main, ...)        \
+    do {                                  \
+        dl::launch_begin(h);              \
+        __VA_ARGS__;                      \
+        dl::launch_end((h), (is_main));   \
+    } while (0)
+
+#define DL_CUDA(h, call)                                                  \
+    do {                                                                  \
+        cudaError_t e_ = (call);                                          \
+        if (e_ != cudaSuccess) return dl::check_cuda((h), e_, #call);     \
+    } while (0)

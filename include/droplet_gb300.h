@@ -1,0 +1,203 @@
+/*
+ * droplet_gb300.h -- C-ABI of the GB300 D3Q15 two-phase droplet step.
+ *
+ * The reference (nakano-gendai/droplet) has no library interface: its hot
+ * path is the subroutine sequence inside the Fortran `program main` of
+ * program/lbm_drop_xy.f90:830-840 (identical at program/lbm_drop_iht_xy.f90:1016-1026
+ * and program/lbm_omp_drop.f90:827-837), with state in module-level arrays.
+ * Each entry point below replaces one piece of that sequence; the comment on
+ * each names the reference lines it stands in for.
+ *
+ * Conventions
+ *  - Every function returns an int status: DL_OK (0) or a negative DL_ERR_*.
+ *  - Scalar fields (phi, u1, u2, u3, p, forces) are host arrays of nx*ny*nz
+ *    doubles, x fastest, then y, then z: the Fortran order of
+ *    phi_procs(x,y,z) in the reference, i.e. C order [z][y][x].
+ *  - Populations are host arrays of 15*nx*ny*nz doubles with the direction
+ *    index fastest: the reference's f_procs(1:15,x,y,z) layout.
+ *  - The library owns all device memory; the caller owns host arrays.
+ *    Calls on one handle must not overlap (single-threaded per handle).
+ *  - Directions i = 0..14 here are the reference's i = 1..15.
+ */
+#ifndef DROPLET_GB300_H
+#define DROPLET_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------- */
+#define DL_OK               0
+#define DL_ERR_ARG         -1   /* bad argument (null pointer, size, mode) */
+#define DL_ERR_CUDA        -2   /* a CUDA runtime call failed */
+#define DL_ERR_ALLOC       -3   /* device or host allocation failed */
+#define DL_ERR_NAN         -4   /* the NaN/Inf watchdog tripped during a step */
+#define DL_ERR_TIMEOUT     -5   /* a bounded device-side wait ran out */
+#define DL_ERR_STATE       -6   /* call out of order (e.g. step before fields) */
+#define DL_ERR_UNSUPPORTED -7   /* option not available in this form */
+
+/* ---- storage / arithmetic forms ------------------------------------------ */
+#define DL_FORM_FP64  64  /* plain form: FP64 storage and arithmetic in the
+                             reference's evaluation order (no FMA contraction) */
+#define DL_FORM_FP32  32  /* FP32 arithmetic; populations stored in FP32 as
+                             deviations from the bulk equilibrium at phi1, p=1/3 */
+#define DL_FORM_FP16  16  /* FP32 arithmetic; populations stored as scaled
+                             FP16 deviations; FP64 for conservation sums */
+
+/* ---- body-force modes ------------------------------------------------------ */
+#define DL_FORCE_NONE      0
+#define DL_FORCE_STATIC    1  /* caller-given Fx,Fy,Fz held fixed in time:
+                                 externalforce, program/lbm_drop_xy.f90:668-693 */
+#define DL_FORCE_SPECTRAL  2  /* constant-injection band forcing recomputed from
+                                 u every step: externalforce,
+                                 program/lbm_drop_iht_xy.f90:722-842 */
+
+/* ---- viscosity interpolation ----------------------------------------------- */
+#define DL_VISC_MINMAX 0  /* nu from the previous step's global phi min/max:
+                             physics, program/lbm_drop_xy.f90:559-587 */
+#define DL_VISC_FIXED  1  /* nu from the fixed phi1..phi2 range:
+                             ini_op, program/lbm_drop_xy.f90:254-285 */
+
+/* Physical and numerical parameters. Names follow the reference's
+ * `module globals` (program/lbm_drop_xy.f90:10-59). */
+typedef struct dl_params {
+    double ds;          /* lattice spacing */
+    double tauf;        /* relaxation time of f (order parameter) */
+    double kappaf;      /* interface-thickness parameter */
+    double kappag;      /* surface-tension parameter */
+    double phi1, phi2;  /* continuous / dispersed phase order parameter */
+    double a, b, T;     /* van der Waals constants of p0(phi) */
+    double nu1, nu2;    /* kinematic viscosity of phase 1 / phase 2 */
+    double Anu;         /* velocity-gradient correction in geq */
+    double Cs, delta;   /* Smagorinsky constant and filter width (les != 0) */
+    double wall_u[3];   /* top-wall velocity; the bottom wall moves with -wall_u */
+    double eps;         /* energy injection rate of the spectral forcing */
+    int64_t wall_start; /* first step (1-based) at which the walls move */
+    int32_t visc_mode;  /* DL_VISC_* */
+    int32_t les;        /* nonzero: Smagorinsky eddy viscosity in tau_g */
+    int32_t walls;      /* nonzero: moving-wall bounce-back of g at z=0, z=nz-1 */
+    int32_t kc;         /* spectral forcing acts on 1 <= |k| < kc */
+} dl_params;
+
+/* FP64 diagnostics over the whole domain (compensated sums). */
+typedef struct dl_diag {
+    double phi_sum;      /* sum of phi */
+    double p_sum;        /* sum of p */
+    double mom[3];       /* sum of u */
+    double ke;           /* 1/2 sum |u|^2 */
+    double diss;         /* sum of 2 nu(phi) S:S (stencil strain) */
+    double vol_count;    /* number of sites with phi > (phi1+phi2)/2 */
+    double vol_smooth;   /* sum of (phi-phi1)/(phi2-phi1) */
+    double phi_min, phi_max;
+    double p_in, n_in;   /* sum of p and count where (phi-phi1)/(phi2-phi1) > 0.95 */
+    double p_out, n_out; /* sum of p and count where it is < 0.05 */
+    double w_sum;        /* second-moment tensor of w = (phi-phi1)/(phi2-phi1) */
+    double w_x[3];       /* sum w*x_a */
+    double w_xx[6];      /* sum w*x_a*x_b : xx, yy, zz, xy, xz, yz */
+    int64_t step;        /* steps taken since dl_create */
+    int32_t nan_flag;    /* nonzero if the watchdog saw NaN/Inf */
+    int32_t pad_;
+} dl_diag;
+
+/* Launch accounting of the library's own kernels (for benchmarks). */
+typedef struct dl_profile_stats {
+    double main_ms;          /* summed device time of the fused step kernel */
+    double total_ms;         /* summed device time of every timed launch */
+    int64_t main_launches;   /* launches of the fused step kernel */
+    int64_t timed_launches;  /* launches bracketed by events */
+    int64_t launches;        /* all kernel launches issued since the last read */
+} dl_profile_stats;
+
+typedef struct dl_handle dl_handle;
+
+/* Library version (major*10000 + minor*100 + patch). */
+int dl_version(void);
+
+/* Human-readable text of a status code. */
+const char* dl_status_string(int status);
+
+/* Allocate a whole-domain state on the current CUDA device.
+ * Replaces the allocations of ini/ini_op, program/lbm_drop_xy.f90:131-285,
+ * without the MPI decomposition (:143-185): the domain is resident. */
+int dl_create(const dl_params* params, int nx, int ny, int nz, int form,
+              dl_handle** out);
+
+/* Free all device memory of the handle. */
+int dl_destroy(dl_handle* h);
+
+/* Run subsequent work on this cudaStream_t (NULL: the legacy default stream). */
+int dl_set_stream(dl_handle* h, void* cuda_stream);
+
+/* Upload phi, u1, u2, u3, p (x fastest). Replaces the initial-condition loop
+ * of ini, program/lbm_drop_xy.f90:224-242. */
+int dl_set_fields(dl_handle* h, const double* phi, const double* u1,
+                  const double* u2, const double* u3, const double* p);
+
+/* f <- feq, g <- geq from the current fields, and reset the tau_g
+ * interpolation range to phi1..phi2. Replaces the tail of ini,
+ * program/lbm_drop_xy.f90:244-251, and ini_op, :254-285. */
+int dl_init_equilibrium(dl_handle* h);
+
+/* Select the body force. mode DL_FORCE_STATIC uploads fx, fy, fz (x fastest);
+ * the other modes take NULL. Replaces externalforce + glue(force),
+ * program/lbm_drop_xy.f90:825-827 and program/lbm_drop_iht_xy.f90:1008-1014. */
+int dl_set_force(dl_handle* h, int mode, const double* fx, const double* fy,
+                 const double* fz);
+
+/* Advance nsteps time steps. One step replaces the loop body
+ * program/lbm_drop_xy.f90:830-840 (MPI_boundary, various_cal, gphi_cal,
+ * equilibrium_cal, MPI_boundary_fg, fg_cal, physics) plus, when enabled,
+ * the spectral force of program/lbm_drop_iht_xy.f90:1008-1014, the
+ * Smagorinsky tau_g of program/LES_drop_xy.f90:655-690 and the moving-wall
+ * bounce-back of prototype_program/two-phase/drop8_mpi.f90:642-674. */
+int dl_step(dl_handle* h, int nsteps);
+
+/* Download phi, u1, u2, u3, p (x fastest): the record content of output,
+ * program/lbm_drop_xy.f90:695-719. */
+int dl_get_fields(dl_handle* h, double* phi, double* u1, double* u2,
+                  double* u3, double* p);
+
+/* Download f and g, direction index fastest: the content of outputfg,
+ * program/lbm_drop_xy.f90:721-743 (checkpoint). */
+int dl_get_populations(dl_handle* h, double* f, double* g);
+
+/* Upload f and g (direction fastest) and recompute phi, p, u from them:
+ * resume from a checkpoint, or the precursor read of
+ * program/lbm_drop_xy.f90:789-823 (which recomputes p and u from g). */
+int dl_set_populations(dl_handle* h, const double* f, const double* g);
+
+/* Set / read the step counter (used by the wall start time). */
+int dl_set_step(dl_handle* h, int64_t step);
+int dl_get_step(dl_handle* h, int64_t* step);
+
+/* The phi min/max that the next step's tau_g interpolation will use:
+ * phi_min/phi_max after the MPI_Allreduce, program/lbm_drop_xy.f90:559-574. */
+int dl_get_minmax(dl_handle* h, double* phi_min, double* phi_max);
+
+/* FP64 diagnostics of the current fields; replaces the ad-hoc sums of the
+ * analysis programs (kinetic.d in program/lbm_iht_xy.f90:777-822, the
+ * droplet moments of prototype_program/two-phase/drop8_mpi.f90:812-970). */
+int dl_reduce(dl_handle* h, dl_diag* out);
+
+/* Wait for all work of the handle; returns the first deferred error. */
+int dl_sync(dl_handle* h);
+
+/* Bracket every kernel launch of the handle with CUDA events on its stream
+ * (enable != 0) or stop doing so; resets the counters. The reference times
+ * its loop with MPI_Wtime and writes time.d (program/lbm_drop_xy.f90:785-864);
+ * this is the per-kernel device-side equivalent. */
+int dl_profile(dl_handle* h, int enable);
+
+/* Synchronise, then report and reset the launch counters and event times. */
+int dl_profile_read(dl_handle* h, dl_profile_stats* out);
+
+/* Copy the last error message of the handle into buf (NUL-terminated). */
+int dl_last_error(dl_handle* h, char* buf, int buflen);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DROPLET_GB300_H */
