@@ -42,6 +42,7 @@ SOURCES = {
     "spectral.cu": EXACT,
     "layout.cu": EXACT,
     "reduce.cu": EXACT,
+    "step_fast.cu": FAST,
 }
 
 

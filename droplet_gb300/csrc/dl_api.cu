@@ -107,6 +107,13 @@ struct Staging {
     }
 };
 
+static bool is_fast(const dl_handle* h) { return h->form == DL_FORM_FP32 || h->form == DL_FORM_FP16; }
+
+__global__ void f64_to_f32(const double* __restrict__ a, float* __restrict__ b, long long n) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t < n) b[t] = (float)a[t];
+}
+
 }  // namespace dl
 
 using namespace dl;
@@ -133,7 +140,7 @@ int dl_create(const dl_params* params, int nx, int ny, int nz, int form, dl_hand
     if (!params || !out) return DL_ERR_ARG;
     *out = nullptr;
     if (nx < 3 || ny < 3 || nz < 3) return DL_ERR_ARG;
-    if (form != DL_FORM_FP64) return DL_ERR_UNSUPPORTED;
+    if (form != DL_FORM_FP64 && form != DL_FORM_FP32 && form != DL_FORM_FP16) return DL_ERR_UNSUPPORTED;
     if (params->tauf <= 0.5 || params->ds <= 0.0 || params->phi2 == params->phi1) return DL_ERR_ARG;
     if (params->kc < 0 || params->visc_mode < 0 || params->visc_mode > 1) return DL_ERR_ARG;
     dl_handle* h = new (std::nothrow) dl_handle();
@@ -156,7 +163,7 @@ int dl_create(const dl_params* params, int nx, int ny, int nz, int form, dl_hand
     int rc = DL_OK;
     if (cudaMalloc(&h->d_state, sizeof(DevState)) != cudaSuccess) rc = DL_ERR_ALLOC;
     if (rc == DL_OK) rc = reset_state(h);
-    if (rc == DL_OK) rc = fp64_alloc(h);
+    if (rc == DL_OK) rc = is_fast(h) ? fast_alloc(h) : fp64_alloc(h);
     if (rc == DL_OK) rc = spectral_alloc(h);
     if (rc != DL_OK) {
         dl_destroy(h);
@@ -171,6 +178,7 @@ int dl_destroy(dl_handle* h) {
     cudaSetDevice(h->device);
     if (h->stream) cudaStreamSynchronize(h->stream);
     fp64_free(h);
+    fast_free(h);
     spectral_free(h);
     cudaFree(h->d_state);
     cudaFree(h->d_diag);
@@ -218,10 +226,19 @@ int dl_set_fields(dl_handle* h, const double* phi, const double* u1, const doubl
                   const double* p) {
     if (!h || !phi || !u1 || !u2 || !u3 || !p) return DL_ERR_ARG;
     const size_t N = h->N;
+    Staging st;
     double* d = h->mac64[h->cur];
+    if (is_fast(h)) {
+        DL_CUDA(h, cudaMalloc(&st.d, 5 * N * sizeof(double)));
+        d = st.d;
+    }
     const double* src[5] = {phi, u1, u2, u3, p};
     for (int k = 0; k < 5; ++k)
         DL_CUDA(h, cudaMemcpyAsync(d + k * N, src[k], N * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    if (is_fast(h)) {
+        int rc = fast_set_fields(h, d);
+        if (rc != DL_OK) return rc;
+    }
     DL_CUDA(h, cudaStreamSynchronize(h->stream));
     h->fields_set = true;
     return DL_OK;
@@ -230,7 +247,14 @@ int dl_set_fields(dl_handle* h, const double* phi, const double* u1, const doubl
 int dl_get_fields(dl_handle* h, double* phi, double* u1, double* u2, double* u3, double* p) {
     if (!h || !phi || !u1 || !u2 || !u3 || !p) return DL_ERR_ARG;
     const size_t N = h->N;
+    Staging st;
     const double* d = h->mac64[h->cur];
+    if (is_fast(h)) {
+        DL_CUDA(h, cudaMalloc(&st.d, 5 * N * sizeof(double)));
+        int rc = fast_get_fields(h, st.d);
+        if (rc != DL_OK) return rc;
+        d = st.d;
+    }
     double* dst[5] = {phi, u1, u2, u3, p};
     for (int k = 0; k < 5; ++k)
         DL_CUDA(h, cudaMemcpyAsync(dst[k], d + k * N, N * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
@@ -243,7 +267,7 @@ int dl_init_equilibrium(dl_handle* h) {
     if (!h->fields_set) return set_error(h, DL_ERR_STATE, "dl_init_equilibrium before dl_set_fields");
     int rc = set_minmax(h, h->P.phi1, h->P.phi2);
     if (rc != DL_OK) return rc;
-    rc = fp64_init_equilibrium(h);
+    rc = is_fast(h) ? fast_init_equilibrium(h) : fp64_init_equilibrium(h);
     if (rc != DL_OK) return rc;
     DL_CUDA(h, cudaStreamSynchronize(h->stream));
     h->eq_init = true;
@@ -256,13 +280,25 @@ int dl_set_force(dl_handle* h, int mode, const double* fx, const double* fy, con
     if (mode == DL_FORCE_STATIC) {
         if (!fx || !fy || !fz) return DL_ERR_ARG;
         const double* src[3] = {fx, fy, fz};
-        for (int k = 0; k < 3; ++k)
-            DL_CUDA(h, cudaMemcpyAsync(h->force64 + k * N, src[k], N * sizeof(double), cudaMemcpyHostToDevice,
-                                       h->stream));
+        if (is_fast(h)) {
+            Staging st;
+            DL_CUDA(h, cudaMalloc(&st.d, 3 * N * sizeof(double)));
+            for (int k = 0; k < 3; ++k)
+                DL_CUDA(h, cudaMemcpyAsync(st.d + k * N, src[k], N * sizeof(double), cudaMemcpyHostToDevice,
+                                           h->stream));
+            f64_to_f32<<<(unsigned)((3 * N + 255) / 256), 256, 0, h->stream>>>(st.d, h->force32, (long long)(3 * N));
+            DL_CUDA(h, cudaGetLastError());
+            DL_CUDA(h, cudaStreamSynchronize(h->stream));
+        } else {
+            for (int k = 0; k < 3; ++k)
+                DL_CUDA(h, cudaMemcpyAsync(h->force64 + k * N, src[k], N * sizeof(double), cudaMemcpyHostToDevice,
+                                           h->stream));
+        }
     } else if (mode == DL_FORCE_NONE || mode == DL_FORCE_SPECTRAL) {
         if (mode == DL_FORCE_SPECTRAL && (h->P.kc < 2 || h->sp.K < 1))
             return set_error(h, DL_ERR_ARG, "spectral forcing needs kc >= 2");
-        DL_CUDA(h, cudaMemsetAsync(h->force64, 0, 3 * N * sizeof(double), h->stream));
+        if (is_fast(h)) DL_CUDA(h, cudaMemsetAsync(h->force32, 0, 3 * N * sizeof(float), h->stream));
+        else DL_CUDA(h, cudaMemsetAsync(h->force64, 0, 3 * N * sizeof(double), h->stream));
     } else {
         return DL_ERR_ARG;
     }
@@ -275,7 +311,7 @@ int dl_step(dl_handle* h, int nsteps) {
     if (!h || nsteps < 0) return DL_ERR_ARG;
     if (!h->eq_init) return set_error(h, DL_ERR_STATE, "dl_step before dl_init_equilibrium / dl_set_populations");
     for (int k = 0; k < nsteps; ++k) {
-        int rc = fp64_step(h);
+        int rc = is_fast(h) ? fast_step(h) : fp64_step(h);
         if (rc != DL_OK) return rc;
     }
     return DL_OK;
@@ -285,6 +321,15 @@ int dl_get_populations(dl_handle* h, double* f, double* g) {
     if (!h || !f || !g) return DL_ERR_ARG;
     const size_t bytes = Q * h->N * sizeof(double);
     Staging st;
+    if (is_fast(h)) {
+        DL_CUDA(h, cudaMalloc(&st.d, 2 * bytes));
+        int rc = fast_get_populations(h, st.d, st.d + Q * h->N);
+        if (rc != DL_OK) return rc;
+        DL_CUDA(h, cudaMemcpyAsync(f, st.d, bytes, cudaMemcpyDeviceToHost, h->stream));
+        DL_CUDA(h, cudaMemcpyAsync(g, st.d + Q * h->N, bytes, cudaMemcpyDeviceToHost, h->stream));
+        DL_CUDA(h, cudaStreamSynchronize(h->stream));
+        return DL_OK;
+    }
     DL_CUDA(h, cudaMalloc(&st.d, bytes));
     int rc = soa_to_aos(h, h->f64[h->cur], st.d);
     if (rc != DL_OK) return rc;
@@ -301,6 +346,17 @@ int dl_set_populations(dl_handle* h, const double* f, const double* g) {
     if (!h || !f || !g) return DL_ERR_ARG;
     const size_t bytes = Q * h->N * sizeof(double);
     Staging st;
+    if (is_fast(h)) {
+        DL_CUDA(h, cudaMalloc(&st.d, 2 * bytes));
+        DL_CUDA(h, cudaMemcpyAsync(st.d, f, bytes, cudaMemcpyHostToDevice, h->stream));
+        DL_CUDA(h, cudaMemcpyAsync(st.d + Q * h->N, g, bytes, cudaMemcpyHostToDevice, h->stream));
+        int rc = fast_set_populations(h, st.d, st.d + Q * h->N);
+        if (rc != DL_OK) return rc;
+        DL_CUDA(h, cudaStreamSynchronize(h->stream));
+        h->fields_set = true;
+        h->eq_init = true;
+        return DL_OK;
+    }
     DL_CUDA(h, cudaMalloc(&st.d, bytes));
     DL_CUDA(h, cudaMemcpyAsync(st.d, f, bytes, cudaMemcpyHostToDevice, h->stream));
     int rc = aos_to_soa(h, st.d, h->f64[h->cur]);
@@ -350,7 +406,7 @@ int dl_sync(dl_handle* h) {
 
 int dl_reduce(dl_handle* h, dl_diag* out) {
     if (!h || !out) return DL_ERR_ARG;
-    int rc = reduce_fields(h, h->mac64[h->cur], out);
+    int rc = is_fast(h) ? reduce_fields_f32(h, h->mac32[h->cur], out) : reduce_fields(h, h->mac64[h->cur], out);
     if (rc != DL_OK) return rc;
     DevState s;
     DL_CUDA(h, cudaMemcpy(&s, h->d_state, sizeof(s), cudaMemcpyDeviceToHost));

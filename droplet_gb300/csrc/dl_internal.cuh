@@ -85,6 +85,7 @@ struct SpectralPlan {
     double* d_a1;     // [3][2K+1][ny*nz] complex   (x stage)
     double* d_uh;     // [3][2K+1][2K+1][K+1] complex (band coefficients, /N)
     double* d_b2;     // [3][2K+1][ny*nz] complex   (synthesis, x pending)
+    float* d_twxf;    // FP32 copy of d_twx
 };
 
 }  // namespace dl
@@ -117,8 +118,9 @@ struct dl_handle {
     // reduced precision forms (FP32 / FP16 storage)
     void* fs[2];             // populations, storage type of the form
     void* gs[2];
-    float* mac32[2];         // [5][N]
-    double* force32_unused;
+    float* mac32[2];         // [5][N]: phi - phi1, u1, u2, u3, p - 1/3
+    float* force32;          // [3][N]
+    int lz;                  // z planes per block of the fused kernel
 
     dl::SpectralPlan sp;
     double* d_diag;          // diagnostics partial sums
@@ -146,11 +148,23 @@ int spectral_alloc(dl_handle* h);
 void spectral_free(dl_handle* h);
 int spectral_force_fp64(dl_handle* h, const double* d_u1, const double* d_u2, const double* d_u3,
                         double* d_fx, double* d_fy, double* d_fz);
+int spectral_force_f32(dl_handle* h, const float* d_u1, const float* d_u2, const float* d_u3,
+                       float* d_fx, float* d_fy, float* d_fz);
+// fp32 / fp16-storage forms (step_fast.cu)
+int fast_alloc(dl_handle* h);
+void fast_free(dl_handle* h);
+int fast_set_fields(dl_handle* h, const double* d_fields);
+int fast_get_fields(dl_handle* h, double* d_fields);
+int fast_init_equilibrium(dl_handle* h);
+int fast_get_populations(dl_handle* h, double* d_f, double* d_g);
+int fast_set_populations(dl_handle* h, const double* d_f, const double* d_g);
+int fast_step(dl_handle* h);
 // transposes (layout.cu)
 int soa_to_aos(dl_handle* h, const double* d_soa, double* d_aos);
 int aos_to_soa(dl_handle* h, const double* d_aos, double* d_soa);
 // diagnostics (reduce.cu)
 int reduce_fields(dl_handle* h, const double* d_mac, dl_diag* out);
+int reduce_fields_f32(dl_handle* h, const float* d_mac, dl_diag* out);
 
 int set_error(dl_handle* h, int code, const char* fmt, ...);
 // bracket one kernel launch: counts it and, when profiling, records events

@@ -26,6 +26,7 @@ struct RedArgs {
     int nx, ny, nz;
     long long N;
     double phi1, phi2, nu1, dnu, graddiv;
+    double phi_off, p_off;  // stored phi and p are phi - phi_off, p - p_off
     double* part;
 };
 
@@ -43,9 +44,9 @@ __global__ void __launch_bounds__(RED_THREADS) reduce_partials(const T* __restri
         const int x = (int)(s - t * a.nx);
         const int z = (int)(t / a.ny);
         const int y = (int)(t - (long long)z * a.ny);
-        const double ph = (double)mac[s];
+        const double ph = a.phi_off + (double)mac[s];
         const double u1 = (double)mac[N + s], u2 = (double)mac[2 * N + s], u3 = (double)mac[3 * N + s];
-        const double p = (double)mac[4 * N + s];
+        const double p = a.p_off + (double)mac[4 * N + s];
         // velocity gradient with the 14-neighbour stencil
         double gu[9];
 #pragma unroll
@@ -161,7 +162,8 @@ __global__ void reduce_final(const double* __restrict__ part, int nblocks, doubl
     out[k] = s + c;
 }
 
-int reduce_fields(dl_handle* h, const double* d_mac, dl_diag* out) {
+template <typename T>
+static int reduce_any(dl_handle* h, const T* d_mac, double phi_off, double p_off, dl_diag* out) {
     if (!h->d_diag) DL_CUDA(h, cudaMalloc(&h->d_diag, sizeof(double) * (RED_BLOCKS * NPART + NPART)));
     RedArgs a;
     memset(&a, 0, sizeof(a));
@@ -174,8 +176,10 @@ int reduce_fields(dl_handle* h, const double* d_mac, dl_diag* out) {
     a.nu1 = h->P.nu1;
     a.dnu = h->P.nu2 - h->P.nu1;
     a.graddiv = 10.0 * h->P.ds;
+    a.phi_off = phi_off;
+    a.p_off = p_off;
     a.part = h->d_diag;
-    DL_LAUNCH(h, false, reduce_partials<double><<<RED_BLOCKS, RED_THREADS, 0, h->stream>>>(d_mac, a));
+    DL_LAUNCH(h, false, reduce_partials<T><<<RED_BLOCKS, RED_THREADS, 0, h->stream>>>(d_mac, a));
     DL_LAUNCH(h, false, reduce_final<<<1, 32, 0, h->stream>>>(h->d_diag, RED_BLOCKS, h->d_diag + RED_BLOCKS * NPART));
     DL_CUDA(h, cudaGetLastError());
     double r[NPART];
@@ -209,6 +213,12 @@ int reduce_fields(dl_handle* h, const double* d_mac, dl_diag* out) {
     out->phi_max = r[NSUM + 1];
     (void)r[23];
     return DL_OK;
+}
+
+int reduce_fields(dl_handle* h, const double* d_mac, dl_diag* out) { return reduce_any<double>(h, d_mac, 0.0, 0.0, out); }
+
+int reduce_fields_f32(dl_handle* h, const float* d_mac, dl_diag* out) {
+    return reduce_any<float>(h, d_mac, h->P.phi1, 1.0 / 3.0, out);
 }
 
 }  // namespace dl

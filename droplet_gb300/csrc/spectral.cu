@@ -221,6 +221,80 @@ __global__ void sp_synth_x(const SpArgs a) {
     a.fo[c][s] = re;
 }
 
+// FP32 forms: the x stage with one warp per (y, z) row (lanes over x, FP32
+// sums, reduced across the warp), and the x synthesis writing FP32 forces.
+// The small y / z stages and the energy are shared with the FP64 form.
+constexpr int SP_KMAX = 4;  // supports kc <= 5
+
+__global__ void sp_xstage_f32(const float* __restrict__ u1, const float* __restrict__ u2,
+                              const float* __restrict__ u3, double* __restrict__ a1, int nx, int ny, int nz, int K,
+                              const float* __restrict__ tw) {
+    const int lane = threadIdx.x & 31;
+    const long long row = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    if (row >= (long long)ny * nz) return;
+    const int z = (int)(row / ny), y = (int)(row - (long long)z * ny);
+    const int NK = 2 * K + 1;
+    const float* u[3] = {u1, u2, u3};
+    const long long base = ((long long)z * ny + y) * nx;
+    float re[3][2 * SP_KMAX + 1], im[3][2 * SP_KMAX + 1];
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+        for (int k = 0; k < NK; ++k) re[c][k] = im[c][k] = 0.f;
+    for (int x = lane; x < nx; x += 32) {
+        const float v[3] = {u[0][base + x], u[1][base + x], u[2][base + x]};
+        for (int k = 0; k < NK; ++k) {
+            int m = ((k - K) * x) % nx;
+            m = m < 0 ? m + nx : m;
+            const float cs = tw[2 * m], sn = tw[2 * m + 1];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                re[c][k] += v[c] * cs;
+                im[c][k] -= v[c] * sn;
+            }
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+        for (int k = 0; k < NK; ++k) {
+            float r = re[c][k], i = im[c][k];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                r += __shfl_xor_sync(0xffffffffu, r, o);
+                i += __shfl_xor_sync(0xffffffffu, i, o);
+            }
+            if (lane == 0) {
+                double* d = a1 + 2 * ((((long long)c * NK + k) * ny + y) * nz + z);
+                d[0] = (double)r;
+                d[1] = (double)i;
+            }
+        }
+}
+
+__global__ void sp_synth_x_f32(const double* __restrict__ b2, float* __restrict__ fx, float* __restrict__ fy,
+                               float* __restrict__ fz, int nx, int ny, int nz, int K, const float* __restrict__ tw) {
+    const long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long N = (long long)nx * ny * nz;
+    if (s >= N) return;
+    const int x = (int)(s % nx);
+    const long long r = s / nx;
+    const int y = (int)(r % ny), z = (int)(r / ny);
+    const int NK = 2 * K + 1;
+    float out[3] = {0.f, 0.f, 0.f};
+    for (int k = 0; k < NK; ++k) {
+        int m = ((k - K) * x) % nx;
+        m = m < 0 ? m + nx : m;
+        const float cs = tw[2 * m], sn = tw[2 * m + 1];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const double* v = b2 + 2 * ((((long long)c * NK + k) * ny + y) * nz + z);
+            out[c] += (float)v[0] * cs - (float)v[1] * sn;
+        }
+    }
+    fx[s] = out[0];
+    fy[s] = out[1];
+    fz[s] = out[2];
+}
+
 static int upload_twiddle(dl_handle* h, int n, double** d) {
     std::vector<double> t(2 * (size_t)n);
     const double pi = acos(-1.0);
@@ -247,6 +321,17 @@ int spectral_alloc(dl_handle* h) {
     if ((rc = upload_twiddle(h, h->nx, &sp.d_twx)) != DL_OK) return rc;
     if ((rc = upload_twiddle(h, h->ny, &sp.d_twy)) != DL_OK) return rc;
     if ((rc = upload_twiddle(h, h->nz, &sp.d_twz)) != DL_OK) return rc;
+    if (K > SP_KMAX) return set_error(h, DL_ERR_ARG, "kc=%d above the supported maximum %d", h->P.kc, SP_KMAX + 1);
+    {
+        std::vector<float> t(2 * (size_t)h->nx);
+        const double pi = acos(-1.0);
+        for (int m = 0; m < h->nx; ++m) {
+            t[2 * m] = (float)cos(2.0 * pi * m / h->nx);
+            t[2 * m + 1] = (float)sin(2.0 * pi * m / h->nx);
+        }
+        DL_CUDA(h, cudaMalloc(&sp.d_twxf, sizeof(float) * 2 * h->nx));
+        DL_CUDA(h, cudaMemcpy(sp.d_twxf, t.data(), sizeof(float) * 2 * h->nx, cudaMemcpyHostToDevice));
+    }
     const size_t rows = (size_t)h->ny * h->nz;
     DL_CUDA(h, cudaMalloc(&sp.d_a1, sizeof(double) * 2 * 3 * NK * rows));
     DL_CUDA(h, cudaMalloc(&sp.d_b2, sizeof(double) * 2 * 3 * NK * rows));
@@ -271,6 +356,7 @@ void spectral_free(dl_handle* h) {
     cudaFree(sp.d_a1);
     cudaFree(sp.d_b2);
     cudaFree(sp.d_uh);
+    cudaFree(sp.d_twxf);
     memset(&sp, 0, sizeof(sp));
 }
 
@@ -318,6 +404,27 @@ int spectral_force_fp64(dl_handle* h, const double* u1, const double* u2, const 
     DL_LAUNCH(h, false, sp_synth_z<<<nb(3LL * NK * NK * h->nz, 128), 128, 0, s>>>(a));
     DL_LAUNCH(h, false, sp_synth_y<<<nb(3LL * NK * h->ny * h->nz, 128), 128, 0, s>>>(a));
     DL_LAUNCH(h, false, sp_synth_x<<<nb(3 * N, 256), 256, 0, s>>>(a));
+    DL_CUDA(h, cudaGetLastError());
+    return DL_OK;
+}
+
+int spectral_force_f32(dl_handle* h, const float* u1, const float* u2, const float* u3, float* fx, float* fy,
+                       float* fz) {
+    SpArgs a;
+    fill_sp(h, a);
+    const int NK = 2 * a.K + 1;
+    const long long N = (long long)h->N;
+    cudaStream_t s = h->stream;
+    const long long rows = (long long)h->ny * h->nz;
+    DL_LAUNCH(h, false, sp_xstage_f32<<<nb(rows * 32, 256), 256, 0, s>>>(u1, u2, u3, a.a1, h->nx, h->ny, h->nz, a.K,
+                                                                        h->sp.d_twxf));
+    DL_LAUNCH(h, false, sp_ystage<<<nb(3LL * NK * NK * h->nz, 128), 128, 0, s>>>(a));
+    DL_LAUNCH(h, false, sp_zstage<<<nb(3LL * NK * NK * (a.K + 1), 64), 64, 0, s>>>(a));
+    DL_LAUNCH(h, false, sp_energy<<<1, 32, 0, s>>>(a));
+    DL_LAUNCH(h, false, sp_synth_z<<<nb(3LL * NK * NK * h->nz, 128), 128, 0, s>>>(a));
+    DL_LAUNCH(h, false, sp_synth_y<<<nb(3LL * NK * h->ny * h->nz, 128), 128, 0, s>>>(a));
+    DL_LAUNCH(h, false, sp_synth_x_f32<<<nb(N, 256), 256, 0, s>>>(a.b2, fx, fy, fz, h->nx, h->ny, h->nz, a.K,
+                                                                   h->sp.d_twxf));
     DL_CUDA(h, cudaGetLastError());
     return DL_OK;
 }

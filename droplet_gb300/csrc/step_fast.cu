@@ -1,0 +1,735 @@
+// step_fast.cu -- the reduced-precision forms as ONE fused kernel per time step.
+//
+// Arithmetic is FP32. Populations are stored
+//   FP32 form: as deviations from the bulk equilibrium at phi = phi1, p = 1/3,
+//              u = 0:  df_i = f_i - (H_i phi1 + F_i p0(phi1)),  dg_i = g_i - E_i;
+//   FP16 form: as FP16 residuals against the local part of the equilibrium,
+//              r_i = f_i - (H_i phi + F_i p0(phi) + 3 E_i phi c_i.u) - f_ref,
+//              s_i = g_i - E_i (3p + 3 c_i.u + 4.5 (c_i.u)^2 - 1.5 u^2),
+//              rebuilt from the FP32 moments of the same site when read.
+// The macroscopic fields are FP32: dphi = phi - phi1, u, dp = p - 1/3.
+//
+// One launch does all of program/lbm_drop_xy.f90:830-840 for a block's tile
+// (what the reference spreads over various_cal, gphi_cal, equilibrium_cal,
+// fg_cal and physics, with feq/geq, gradients and fnext materialised):
+//   * the block owns a 32 x 8 column tile and marches up a range of z planes;
+//   * phi (and u for the Smagorinsky strain) are staged plane by plane in
+//     shared memory with a two-cell halo (3-plane ring);
+//   * for every site of the tile plus a one-cell halo a "record" is built
+//     once: dphi, u, the feq bracket dA, S = 3dp - 1.5u^2, 1/tau_g (with the
+//     eddy viscosity), grad(phi), |grad phi|^2 and the body force (3-plane ring);
+//   * each thread pulls its 15 f and 15 g from x - c_i (prefetched into
+//     registers before the record stage), collides each at its source from
+//     that source's record (feq_i, geq_i built on the fly, never stored),
+//     applies the moving-wall bounce-back, takes the moments, stores
+//     populations and fields, and reduces phi min/max; the last block turns
+//     the reduction into the next step's tau_g range.
+#include "dl_internal.cuh"
+#include "dl_device.cuh"
+
+#include <cuda_fp16.h>
+#include <math.h>
+#include <string.h>
+
+namespace dl {
+
+constexpr int TX = 32, TY = 8, NT = TX * TY;
+constexpr int EX1 = TX + 2, EY1 = TY + 2, P1 = EX1 * EY1;  // record plane (1-cell halo)
+constexpr int EX2 = TX + 4, EY2 = TY + 4, P2 = EX2 * EY2;  // staging plane (2-cell halo)
+enum { R_DPHI, R_U1, R_U2, R_U3, R_DA, R_S, R_OMG, R_GX, R_GY, R_GZ, R_GSQ, R_DP0, R_FX, R_FY, R_FZ, NR };
+
+struct FastArgs {
+    int nx, ny, nz, lz;
+    long long N;
+    const float* mac;  // [5][N] dphi, u1, u2, u3, dp
+    float* maco;
+    const void* f;     // [15][N] storage
+    const void* g;
+    void* fo;
+    void* go;
+    const float* force;  // [3][N]
+    DevState* st;
+    float phi1, phi2, omf, kf, kf6, kg, T, a, b, omb1, nu1, dnu, csd, anu23, inv_ds, inv_lap, inv_grad;
+    float fref[Q];   // bulk equilibrium of f (FP32 form offsets)
+    float wall_bot[5], wall_top[5];
+    int walls, visc_fixed;
+    long long step;
+};
+
+__device__ __forceinline__ int pmod(int v, int n) {
+    v %= n;
+    return v < 0 ? v + n : v;
+}
+
+// ---- lattice constants in FP32 -------------------------------------------
+__device__ __forceinline__ constexpr float Ew(int i) { return i == 0 ? 2.0f / 9.0f : (i <= 6 ? 1.0f / 9.0f : 1.0f / 72.0f); }
+__device__ __forceinline__ constexpr float Fw(int i) { return i == 0 ? -7.0f / 3.0f : (i <= 6 ? 1.0f / 3.0f : 1.0f / 24.0f); }
+__device__ __forceinline__ constexpr float c2w(int i) { return i == 0 ? 0.f : (i <= 6 ? 1.f : 3.f); }
+
+// c_i . (a, b, c) with the zero terms dropped; explicit roundings so that the
+// same inputs give the same bits wherever it is inlined
+__device__ __forceinline__ float cdot3(int i, float p, float q, float r) {
+    float s = 0.f;
+    bool any = false;
+    if (cx(i) != 0) {
+        s = cx(i) > 0 ? p : -p;
+        any = true;
+    }
+    if (cy(i) != 0) {
+        const float t = cy(i) > 0 ? q : -q;
+        s = any ? __fadd_rn(s, t) : t;
+        any = true;
+    }
+    if (cz(i) != 0) {
+        const float t = cz(i) > 0 ? r : -r;
+        s = any ? __fadd_rn(s, t) : t;
+    }
+    return s;
+}
+
+template <int AL>
+__device__ __forceinline__ float csumf(const float* v) {
+    float s = 0.f;
+#pragma unroll
+    for (int i = 1; i < Q; ++i) {
+        const int c = AL == 0 ? cx(i) : (AL == 1 ? cy(i) : cz(i));
+        if (c == 1) s += v[i];
+        else if (c == -1) s -= v[i];
+    }
+    return s;
+}
+
+// p0(phi) - p0(phi1) without cancellation:
+// dphi [T / ((1 - b phi)(1 - b phi1)) - a (phi + phi1)]
+__device__ __forceinline__ float site_dp0(const FastArgs& a, float dphi) {
+    const float phi = __fadd_rn(a.phi1, dphi);
+    const float den = __fmul_rn(__fmaf_rn(-a.b, phi, 1.f), a.omb1);
+    const float t = __fdiv_rn(a.T, den);
+    return __fmul_rn(dphi, __fmaf_rn(-a.a, __fadd_rn(phi, a.phi1), t));
+}
+
+__device__ __forceinline__ float site_S(float dp, float u1, float u2, float u3) {
+    const float usq = __fmaf_rn(u3, u3, __fmaf_rn(u2, u2, __fmul_rn(u1, u1)));
+    return __fmaf_rn(-1.5f, usq, __fmul_rn(3.f, dp));
+}
+
+// local part of the equilibria (the FP16 residual basis), deviation form
+__device__ __forceinline__ float fbar(int i, float dphi, float phi, float dp0, float cu) {
+    if (i == 0) return __fmaf_rn(Fw(0), dp0, dphi);
+    return __fmaf_rn(__fmul_rn(3.f * Ew(i), phi), cu, __fmul_rn(Fw(i), dp0));
+}
+__device__ __forceinline__ float gbar(int i, float S, float cu) {
+    return __fmul_rn(Ew(i), __fmaf_rn(cu, __fmaf_rn(4.5f, cu, 3.f), S));
+}
+
+// ---- storage policies ----------------------------------------------------
+template <typename ST>
+struct Pop;
+template <>
+struct Pop<float> {
+    static __device__ __forceinline__ float ld(const void* p, long long i) { return __ldg((const float*)p + i); }
+    static __device__ __forceinline__ void st(void* p, long long i, float v) { ((float*)p)[i] = v; }
+};
+template <>
+struct Pop<__half> {
+    static __device__ __forceinline__ float ld(const void* p, long long i) {
+        return __half2float(__ldg((const __half*)p + i));
+    }
+    static __device__ __forceinline__ void st(void* p, long long i, float v) { ((__half*)p)[i] = __float2half_rn(v); }
+};
+
+// ---- the per-site record ------------------------------------------------------
+struct Rec {
+    float dphi, u1, u2, u3, dA, S, omg, gx, gy, gz, gsq, dp0, Fx, Fy, Fz;
+};
+
+// v[1..14]: dphi at the D3Q15 neighbours; w[c][1..14]: u_c there (LES only)
+template <bool LES>
+__device__ __forceinline__ Rec make_record(const FastArgs& a, float dphi, const float* v, const float (*w)[Q],
+                                           float u1, float u2, float u3, float dp, float mn, float mx) {
+    Rec r;
+    float lap = -14.f * dphi;
+#pragma unroll
+    for (int i = 1; i < Q; ++i) lap += v[i];
+    lap *= a.inv_lap;
+    r.gx = csumf<0>(v) * a.inv_grad;
+    r.gy = csumf<1>(v) * a.inv_grad;
+    r.gz = csumf<2>(v) * a.inv_grad;
+    r.gsq = r.gx * r.gx + r.gy * r.gy + r.gz * r.gz;
+    const float phi = __fadd_rn(a.phi1, dphi);
+    r.dp0 = site_dp0(a, dphi);
+    r.dA = r.dp0 - a.kf * phi * lap - a.kf6 * r.gsq;
+    r.dphi = dphi;
+    r.u1 = u1;
+    r.u2 = u2;
+    r.u3 = u3;
+    r.S = site_S(dp, u1, u2, u3);
+    const float nu = (phi - mn) / (mx - mn) * a.dnu + a.nu1;
+    float nut = 0.f;
+    if (LES) {
+        float gu[9];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            gu[c + 0] = csumf<0>(w[c]) * a.inv_grad;
+            gu[c + 3] = csumf<1>(w[c]) * a.inv_grad;
+            gu[c + 6] = csumf<2>(w[c]) * a.inv_grad;
+        }
+        // S:S with S = (grad u + grad u^T)/2
+        const float sxy = 0.5f * (gu[0 + 3 * 1] + gu[1 + 3 * 0]);
+        const float sxz = 0.5f * (gu[0 + 3 * 2] + gu[2 + 3 * 0]);
+        const float syz = 0.5f * (gu[1 + 3 * 2] + gu[2 + 3 * 1]);
+        const float ss = gu[0] * gu[0] + gu[4] * gu[4] + gu[8] * gu[8] + 2.f * (sxy * sxy + sxz * sxz + syz * syz);
+        nut = a.csd * sqrtf(2.f * ss);
+    }
+    r.omg = 1.f / (0.5f + 3.f * (nu + nut) * a.inv_ds + a.anu23);
+    r.Fx = r.Fy = r.Fz = 0.f;
+    return r;
+}
+
+// collide direction i at its source with record r; fin/gin are the stored values
+template <bool RES, bool FORCE>
+__device__ __forceinline__ void collide_dir(const FastArgs& a, int i, const Rec& r, float fin, float gin, float& fo,
+                                            float& go) {
+    const float phi = __fadd_rn(a.phi1, r.dphi);
+    const float cu = (i == 0) ? 0.f : cdot3(i, r.u1, r.u2, r.u3);
+    const float cg = (i == 0) ? 0.f : cdot3(i, r.gx, r.gy, r.gz);
+    const float cGc = 4.5f * cg * cg - 1.5f * c2w(i) * r.gsq;
+    const float E = Ew(i);
+    if (!RES) {
+        const float dfeq = (i == 0 ? r.dphi : 0.f) + Fw(i) * r.dA + E * (3.f * phi * cu + a.kf * cGc);
+        const float dgeq = E * (r.S + cu * (3.f + 4.5f * cu) + a.kg * cGc);
+        fo = fin + a.omf * (dfeq - fin);
+        go = gin + r.omg * (dgeq - gin);
+    } else {
+        const float fb = fbar(i, r.dphi, phi, r.dp0, cu);
+        const float gb = gbar(i, r.S, cu);
+        const float df = Fw(i) * (r.dA - r.dp0) + E * a.kf * cGc;
+        fo = fb + fin + a.omf * (df - fin);
+        go = gb + gin + r.omg * (E * a.kg * cGc - gin);
+    }
+    if (FORCE && i != 0) go += 3.f * E * cdot3(i, r.Fx, r.Fy, r.Fz);
+}
+
+// ---- the fused step kernel ---------------------------------------------------
+template <typename ST, bool RES, bool LES, bool FORCE>
+__global__ void __launch_bounds__(NT, 2) step_fused(const FastArgs a) {
+    extern __shared__ float smem[];
+    float* s_phi = smem;                            // [3][P2]
+    float* s_u = s_phi + 3 * P2;                    // [3][3][P2] (LES)
+    float* s_rec = s_u + (LES ? 9 * P2 : 0);        // [3][NR][P1]
+    const int tid = threadIdx.x;
+    const int tx = tid % TX, ty = tid / TX;
+    const int nx = a.nx, ny = a.ny, nz = a.nz;
+    const long long N = a.N;
+    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * a.lz;
+    const int z1 = min(z0 + a.lz, nz);
+    float mn, mx;
+    if (a.visc_fixed) {
+        mn = a.phi1;
+        mx = a.phi2;
+    } else {
+        mn = (float)a.st->phi_min;
+        mx = (float)a.st->phi_max;
+    }
+
+    auto stage = [&](int zz) {
+        const int slot = (zz + 3) % 3;
+        const int zw = pmod(zz, nz);
+        for (int k = tid; k < P2; k += NT) {
+            const int ex = k % EX2, ey = k / EX2;
+            const long long s = pmod(x0 - 2 + ex, nx) + (long long)nx * (pmod(y0 - 2 + ey, ny) + (long long)ny * zw);
+            s_phi[slot * P2 + k] = __ldg(a.mac + s);
+            if (LES) {
+                s_u[(slot * 3 + 0) * P2 + k] = __ldg(a.mac + N + s);
+                s_u[(slot * 3 + 1) * P2 + k] = __ldg(a.mac + 2 * N + s);
+                s_u[(slot * 3 + 2) * P2 + k] = __ldg(a.mac + 3 * N + s);
+            }
+        }
+    };
+
+    auto records = [&](int zr) {
+        const int sc = (zr + 3) % 3, sm1 = (zr + 2) % 3, sp1 = (zr + 4) % 3;
+        float* R = s_rec + ((zr + 3) % 3) * NR * P1;
+        const int zw = pmod(zr, nz);
+        for (int k = tid; k < P1; k += NT) {
+            const int ex = k % EX1, ey = k / EX1;
+            const int c2 = (ey + 1) * EX2 + (ex + 1);
+            float v[Q];
+#pragma unroll
+            for (int i = 1; i < Q; ++i) {
+                const int sl = cz(i) == 0 ? sc : (cz(i) > 0 ? sp1 : sm1);
+                v[i] = s_phi[sl * P2 + c2 + cy(i) * EX2 + cx(i)];
+            }
+            const long long s = pmod(x0 - 1 + ex, nx) + (long long)nx * (pmod(y0 - 1 + ey, ny) + (long long)ny * zw);
+            float u1, u2, u3;
+            float w[3][Q];
+            if (LES) {
+                u1 = s_u[(sc * 3 + 0) * P2 + c2];
+                u2 = s_u[(sc * 3 + 1) * P2 + c2];
+                u3 = s_u[(sc * 3 + 2) * P2 + c2];
+#pragma unroll
+                for (int c = 0; c < 3; ++c)
+#pragma unroll
+                    for (int i = 1; i < Q; ++i) {
+                        const int sl = cz(i) == 0 ? sc : (cz(i) > 0 ? sp1 : sm1);
+                        w[c][i] = s_u[(sl * 3 + c) * P2 + c2 + cy(i) * EX2 + cx(i)];
+                    }
+            } else {
+                u1 = __ldg(a.mac + N + s);
+                u2 = __ldg(a.mac + 2 * N + s);
+                u3 = __ldg(a.mac + 3 * N + s);
+            }
+            const float dp = __ldg(a.mac + 4 * N + s);
+            Rec r = make_record<LES>(a, s_phi[sc * P2 + c2], v, w, u1, u2, u3, dp, mn, mx);
+            R[R_DPHI * P1 + k] = r.dphi;
+            R[R_U1 * P1 + k] = r.u1;
+            R[R_U2 * P1 + k] = r.u2;
+            R[R_U3 * P1 + k] = r.u3;
+            R[R_DA * P1 + k] = r.dA;
+            R[R_S * P1 + k] = r.S;
+            R[R_OMG * P1 + k] = r.omg;
+            R[R_GX * P1 + k] = r.gx;
+            R[R_GY * P1 + k] = r.gy;
+            R[R_GZ * P1 + k] = r.gz;
+            R[R_GSQ * P1 + k] = r.gsq;
+            if (RES) R[R_DP0 * P1 + k] = r.dp0;
+            if (FORCE) {
+                R[R_FX * P1 + k] = __ldg(a.force + s);
+                R[R_FY * P1 + k] = __ldg(a.force + N + s);
+                R[R_FZ * P1 + k] = __ldg(a.force + 2 * N + s);
+            }
+        }
+    };
+
+    // prologue: records of planes z0-1 and z0
+    stage(z0 - 2);
+    stage(z0 - 1);
+    stage(z0);
+    __syncthreads();
+    records(z0 - 1);
+    __syncthreads();
+    stage(z0 + 1);
+    __syncthreads();
+    records(z0);
+    __syncthreads();
+
+    const int gxd = x0 + tx, gyd = y0 + ty;
+    const bool act = gxd < nx && gyd < ny;
+    double bmin = INFINITY, bmax = -INFINITY;
+    bool bad = false;
+
+    for (int z = z0; z < z1; ++z) {
+        // populations of the destination plane, pulled from x - c_i
+        float fin[Q], gin[Q];
+        if (act) {
+#pragma unroll
+            for (int i = 0; i < Q; ++i) {
+                const long long src = wrapi(gxd - cx(i), nx) +
+                                      (long long)nx * (wrapi(gyd - cy(i), ny) + (long long)ny * wrapi(z - cz(i), nz));
+                fin[i] = Pop<ST>::ld(a.f, i * N + src);
+                gin[i] = Pop<ST>::ld(a.g, i * N + src);
+            }
+        }
+        stage(z + 2);
+        __syncthreads();
+        records(z + 1);
+        __syncthreads();
+        if (act) {
+            float fo[Q], go[Q];
+#pragma unroll
+            for (int i = 0; i < Q; ++i) {
+                const float* R = s_rec + ((z - cz(i) + 3) % 3) * NR * P1;
+                const int k = (ty + 1 - cy(i)) * EX1 + (tx + 1 - cx(i));
+                Rec r;
+                r.dphi = R[R_DPHI * P1 + k];
+                r.u1 = R[R_U1 * P1 + k];
+                r.u2 = R[R_U2 * P1 + k];
+                r.u3 = R[R_U3 * P1 + k];
+                r.dA = R[R_DA * P1 + k];
+                r.S = R[R_S * P1 + k];
+                r.omg = R[R_OMG * P1 + k];
+                r.gx = R[R_GX * P1 + k];
+                r.gy = R[R_GY * P1 + k];
+                r.gz = R[R_GZ * P1 + k];
+                r.gsq = R[R_GSQ * P1 + k];
+                r.dp0 = RES ? R[R_DP0 * P1 + k] : 0.f;
+                if (FORCE) {
+                    r.Fx = R[R_FX * P1 + k];
+                    r.Fy = R[R_FY * P1 + k];
+                    r.Fz = R[R_FZ * P1 + k];
+                } else {
+                    r.Fx = r.Fy = r.Fz = 0.f;
+                }
+                collide_dir<RES, FORCE>(a, i, r, fin[i], gin[i], fo[i], go[i]);
+            }
+            if (a.walls) {
+                // bounce_back_LBM, prototype_program/two-phase/drop8_mpi.f90:651-671
+                if (z == 0) {
+                    go[3] = go[6] - a.wall_bot[0];
+                    go[7] = go[11] - a.wall_bot[1];
+                    go[8] = go[12] - a.wall_bot[2];
+                    go[9] = go[13] - a.wall_bot[3];
+                    go[14] = go[10] - a.wall_bot[4];
+                }
+                if (z == nz - 1) {
+                    go[6] = go[3] - a.wall_top[0];
+                    go[10] = go[14] - a.wall_top[1];
+                    go[11] = go[7] - a.wall_top[2];
+                    go[12] = go[8] - a.wall_top[3];
+                    go[13] = go[9] - a.wall_top[4];
+                }
+            }
+            // moments (physics, program/lbm_drop_xy.f90:541-552)
+            float dphin = 0.f, dpn = 0.f, u1n = 0.f, u2n = 0.f, u3n = 0.f;
+#pragma unroll
+            for (int i = 0; i < Q; ++i) {
+                dphin += fo[i];
+                dpn += go[i];
+                if (cx(i) == 1) u1n += go[i];
+                else if (cx(i) == -1) u1n -= go[i];
+                if (cy(i) == 1) u2n += go[i];
+                else if (cy(i) == -1) u2n -= go[i];
+                if (cz(i) == 1) u3n += go[i];
+                else if (cz(i) == -1) u3n -= go[i];
+            }
+            dpn *= (1.0f / 3.0f);
+            const long long d = gxd + (long long)nx * (gyd + (long long)ny * z);
+            if (RES) {
+                const float phin = __fadd_rn(a.phi1, dphin);
+                const float dp0n = site_dp0(a, dphin);
+                const float Sn = site_S(dpn, u1n, u2n, u3n);
+#pragma unroll
+                for (int i = 0; i < Q; ++i) {
+                    const float cu = (i == 0) ? 0.f : cdot3(i, u1n, u2n, u3n);
+                    Pop<ST>::st(a.fo, i * N + d, fo[i] - fbar(i, dphin, phin, dp0n, cu));
+                    Pop<ST>::st(a.go, i * N + d, go[i] - gbar(i, Sn, cu));
+                }
+            } else {
+#pragma unroll
+                for (int i = 0; i < Q; ++i) {
+                    Pop<ST>::st(a.fo, i * N + d, fo[i]);
+                    Pop<ST>::st(a.go, i * N + d, go[i]);
+                }
+            }
+            a.maco[d] = dphin;
+            a.maco[N + d] = u1n;
+            a.maco[2 * N + d] = u2n;
+            a.maco[3 * N + d] = u3n;
+            a.maco[4 * N + d] = dpn;
+            const float phin_f = a.phi1 + dphin;
+            if (phin_f == phin_f) {
+                bmin = fmin(bmin, (double)phin_f);
+                bmax = fmax(bmax, (double)phin_f);
+            }
+            bad |= !(isfinite(dphin) && isfinite(dpn) && isfinite(u1n) && isfinite(u2n) && isfinite(u3n));
+        }
+    }
+    minmax_block_and_finalize<float>(a.st, bmin, bmax, a.maco, a.phi1, N, (double)a.phi1, (double)a.phi2, bad,
+                                     a.step);
+}
+
+// ---- initial populations f = feq, g = geq at every site (ini :244-251) -------
+template <typename ST, bool RES>
+__global__ void __launch_bounds__(256) init_fast(const FastArgs a) {
+    const long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (s >= a.N) return;
+    const long long N = a.N;
+    const long long t = s / a.nx;
+    const int x = (int)(s - t * a.nx);
+    const int z = (int)(t / a.ny);
+    const int y = (int)(t - (long long)z * a.ny);
+    float v[Q];
+#pragma unroll
+    for (int i = 1; i < Q; ++i) {
+        const long long nb = wrapi(x + cx(i), a.nx) +
+                             (long long)a.nx * (wrapi(y + cy(i), a.ny) + (long long)a.ny * wrapi(z + cz(i), a.nz));
+        v[i] = a.mac[nb];
+    }
+    const float u1 = a.mac[N + s], u2 = a.mac[2 * N + s], u3 = a.mac[3 * N + s], dp = a.mac[4 * N + s];
+    const Rec r = make_record<false>(a, a.mac[s], v, nullptr, u1, u2, u3, dp, a.phi1, a.phi2);
+    const float phi = __fadd_rn(a.phi1, r.dphi);
+#pragma unroll
+    for (int i = 0; i < Q; ++i) {
+        const float cu = (i == 0) ? 0.f : cdot3(i, u1, u2, u3);
+        const float cg = (i == 0) ? 0.f : cdot3(i, r.gx, r.gy, r.gz);
+        const float cGc = 4.5f * cg * cg - 1.5f * c2w(i) * r.gsq;
+        const float E = Ew(i);
+        const float dfeq = (i == 0 ? r.dphi : 0.f) + Fw(i) * r.dA + E * (3.f * phi * cu + a.kf * cGc);
+        const float dgeq = E * (r.S + cu * (3.f + 4.5f * cu) + a.kg * cGc);
+        if (RES) {
+            Pop<ST>::st(a.fo, i * N + s, dfeq - fbar(i, r.dphi, phi, r.dp0, cu));
+            Pop<ST>::st(a.go, i * N + s, dgeq - gbar(i, r.S, cu));
+        } else {
+            Pop<ST>::st(a.fo, i * N + s, dfeq);
+            Pop<ST>::st(a.go, i * N + s, dgeq);
+        }
+    }
+}
+
+// ---- host <-> device conversions -------------------------------------------
+// doubles [5][N] (phi, u1, u2, u3, p) -> float deviations
+__global__ void fields_to_fast(const double* __restrict__ d, float* __restrict__ m, long long N, double phi1) {
+    const long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (s >= N) return;
+    m[s] = (float)(d[s] - phi1);
+    m[N + s] = (float)d[N + s];
+    m[2 * N + s] = (float)d[2 * N + s];
+    m[3 * N + s] = (float)d[3 * N + s];
+    m[4 * N + s] = (float)(d[4 * N + s] - 1.0 / 3.0);
+}
+
+__global__ void fast_to_fields(const float* __restrict__ m, double* __restrict__ d, long long N, double phi1) {
+    const long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (s >= N) return;
+    d[s] = phi1 + (double)m[s];
+    d[N + s] = (double)m[N + s];
+    d[2 * N + s] = (double)m[2 * N + s];
+    d[3 * N + s] = (double)m[3 * N + s];
+    d[4 * N + s] = 1.0 / 3.0 + (double)m[4 * N + s];
+}
+
+// stored populations -> full f, g as doubles, direction fastest
+template <typename ST, bool RES>
+__global__ void pops_to_host(const FastArgs a, double* __restrict__ fa, double* __restrict__ ga) {
+    const long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (s >= a.N) return;
+    const long long N = a.N;
+    const float dphi = a.mac[s], u1 = a.mac[N + s], u2 = a.mac[2 * N + s], u3 = a.mac[3 * N + s];
+    const float dp = a.mac[4 * N + s];
+    const float phi = __fadd_rn(a.phi1, dphi);
+    const float dp0 = site_dp0(a, dphi);
+    const float S = site_S(dp, u1, u2, u3);
+    const double E[3] = {2.0 / 9.0, 1.0 / 9.0, 1.0 / 72.0};
+#pragma unroll
+    for (int i = 0; i < Q; ++i) {
+        double fv = (double)Pop<ST>::ld(a.f, i * N + s);
+        double gv = (double)Pop<ST>::ld(a.g, i * N + s);
+        if (RES) {
+            const float cu = (i == 0) ? 0.f : cdot3(i, u1, u2, u3);
+            fv += (double)fbar(i, dphi, phi, dp0, cu);
+            gv += (double)gbar(i, S, cu);
+        }
+        fa[s * Q + i] = fv + (double)a.fref[i];
+        ga[s * Q + i] = gv + E[wclass(i)];
+    }
+}
+
+// full f, g (direction fastest, doubles) -> moments and stored populations
+template <typename ST, bool RES>
+__global__ void pops_from_host(const FastArgs a, const double* __restrict__ fa, const double* __restrict__ ga) {
+    const long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (s >= a.N) return;
+    const long long N = a.N;
+    const double E[3] = {2.0 / 9.0, 1.0 / 9.0, 1.0 / 72.0};
+    double ph = 0.0, pp = 0.0, m1 = 0.0, m2 = 0.0, m3 = 0.0;
+    float df[Q], dg[Q];
+#pragma unroll
+    for (int i = 0; i < Q; ++i) {
+        const double fv = fa[s * Q + i], gv = ga[s * Q + i];
+        ph += fv;
+        pp += gv / 3.0;
+        m1 += cx(i) * gv;
+        m2 += cy(i) * gv;
+        m3 += cz(i) * gv;
+        df[i] = (float)(fv - (double)a.fref[i]);
+        dg[i] = (float)(gv - E[wclass(i)]);
+    }
+    const float dphi = (float)(ph - (double)a.phi1);
+    const float u1 = (float)m1, u2 = (float)m2, u3 = (float)m3, dp = (float)(pp - 1.0 / 3.0);
+    a.maco[s] = dphi;
+    a.maco[N + s] = u1;
+    a.maco[2 * N + s] = u2;
+    a.maco[3 * N + s] = u3;
+    a.maco[4 * N + s] = dp;
+    const float phi = __fadd_rn(a.phi1, dphi);
+    const float dp0 = site_dp0(a, dphi);
+    const float S = site_S(dp, u1, u2, u3);
+#pragma unroll
+    for (int i = 0; i < Q; ++i) {
+        float fv = df[i], gv = dg[i];
+        if (RES) {
+            const float cu = (i == 0) ? 0.f : cdot3(i, u1, u2, u3);
+            fv -= fbar(i, dphi, phi, dp0, cu);
+            gv -= gbar(i, S, cu);
+        }
+        Pop<ST>::st(a.fo, i * N + s, fv);
+        Pop<ST>::st(a.go, i * N + s, gv);
+    }
+}
+
+// ---- host side ---------------------------------------------------------------------
+static size_t smem_bytes(bool les) { return sizeof(float) * (3 * P2 + (les ? 9 * P2 : 0) + 3 * NR * P1); }
+
+static void fill_fast(dl_handle* h, FastArgs& a) {
+    const dl_params& P = h->P;
+    memset(&a, 0, sizeof(a));
+    a.nx = h->nx;
+    a.ny = h->ny;
+    a.nz = h->nz;
+    a.lz = h->lz > 0 ? h->lz : 16;
+    a.N = (long long)h->N;
+    a.st = h->d_state;
+    a.phi1 = (float)P.phi1;
+    a.phi2 = (float)P.phi2;
+    a.omf = (float)(1.0 / P.tauf);
+    a.kf = (float)P.kappaf;
+    a.kf6 = (float)(P.kappaf / 6.0);
+    a.kg = (float)P.kappag;
+    a.T = (float)P.T;
+    a.a = (float)P.a;
+    a.b = (float)P.b;
+    a.omb1 = (float)(1.0 - P.b * P.phi1);
+    a.nu1 = (float)P.nu1;
+    a.dnu = (float)(P.nu2 - P.nu1);
+    a.csd = (float)(P.Cs * P.Cs * P.delta * P.delta);
+    a.anu23 = (float)((2.0 / 3.0) * P.Anu);
+    a.inv_ds = (float)(1.0 / P.ds);
+    a.inv_lap = (float)(1.0 / (5.0 * P.ds * P.ds));
+    a.inv_grad = (float)(1.0 / (10.0 * P.ds));
+    const double p0ref = P.phi1 * P.T / (1.0 - P.b * P.phi1) - P.a * P.phi1 * P.phi1;
+    for (int i = 0; i < Q; ++i) a.fref[i] = (float)((i == 0 ? P.phi1 : 0.0) + h->lc.F[i] * p0ref);
+    a.walls = P.walls ? 1 : 0;
+    a.visc_fixed = (P.visc_mode == DL_VISC_FIXED) ? 1 : 0;
+    a.force = h->force32;
+}
+
+static inline unsigned nblk(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+
+int fast_alloc(dl_handle* h) {
+    const size_t N = h->N;
+    const size_t es = (h->form == DL_FORM_FP16) ? sizeof(__half) : sizeof(float);
+    for (int k = 0; k < 2; ++k) {
+        DL_CUDA(h, cudaMalloc(&h->fs[k], es * Q * N));
+        DL_CUDA(h, cudaMalloc(&h->gs[k], es * Q * N));
+        DL_CUDA(h, cudaMalloc(&h->mac32[k], sizeof(float) * 5 * N));
+        DL_CUDA(h, cudaMemsetAsync(h->fs[k], 0, es * Q * N, h->stream));
+        DL_CUDA(h, cudaMemsetAsync(h->gs[k], 0, es * Q * N, h->stream));
+        DL_CUDA(h, cudaMemsetAsync(h->mac32[k], 0, sizeof(float) * 5 * N, h->stream));
+    }
+    DL_CUDA(h, cudaMalloc(&h->force32, sizeof(float) * 3 * N));
+    DL_CUDA(h, cudaMemsetAsync(h->force32, 0, sizeof(float) * 3 * N, h->stream));
+    if (h->lz <= 0) h->lz = 16;
+    return DL_OK;
+}
+
+void fast_free(dl_handle* h) {
+    for (int k = 0; k < 2; ++k) {
+        cudaFree(h->fs[k]);
+        cudaFree(h->gs[k]);
+        cudaFree(h->mac32[k]);
+        h->fs[k] = h->gs[k] = nullptr;
+        h->mac32[k] = nullptr;
+    }
+    cudaFree(h->force32);
+    h->force32 = nullptr;
+}
+
+int fast_set_fields(dl_handle* h, const double* d_fields) {
+    fields_to_fast<<<nblk(h->N, 256), 256, 0, h->stream>>>(d_fields, h->mac32[h->cur], (long long)h->N, h->P.phi1);
+    DL_CUDA(h, cudaGetLastError());
+    return DL_OK;
+}
+
+int fast_get_fields(dl_handle* h, double* d_fields) {
+    fast_to_fields<<<nblk(h->N, 256), 256, 0, h->stream>>>(h->mac32[h->cur], d_fields, (long long)h->N, h->P.phi1);
+    DL_CUDA(h, cudaGetLastError());
+    return DL_OK;
+}
+
+int fast_init_equilibrium(dl_handle* h) {
+    FastArgs a;
+    fill_fast(h, a);
+    a.mac = h->mac32[h->cur];
+    a.fo = h->fs[h->cur];
+    a.go = h->gs[h->cur];
+    if (h->form == DL_FORM_FP16) DL_LAUNCH(h, false, (init_fast<__half, true><<<nblk(a.N, 256), 256, 0, h->stream>>>(a)));
+    else DL_LAUNCH(h, false, (init_fast<float, false><<<nblk(a.N, 256), 256, 0, h->stream>>>(a)));
+    DL_CUDA(h, cudaGetLastError());
+    return DL_OK;
+}
+
+int fast_get_populations(dl_handle* h, double* d_f, double* d_g) {
+    FastArgs a;
+    fill_fast(h, a);
+    a.mac = h->mac32[h->cur];
+    a.f = h->fs[h->cur];
+    a.g = h->gs[h->cur];
+    if (h->form == DL_FORM_FP16) pops_to_host<__half, true><<<nblk(a.N, 256), 256, 0, h->stream>>>(a, d_f, d_g);
+    else pops_to_host<float, false><<<nblk(a.N, 256), 256, 0, h->stream>>>(a, d_f, d_g);
+    DL_CUDA(h, cudaGetLastError());
+    return DL_OK;
+}
+
+int fast_set_populations(dl_handle* h, const double* d_f, const double* d_g) {
+    FastArgs a;
+    fill_fast(h, a);
+    a.maco = h->mac32[h->cur];
+    a.fo = h->fs[h->cur];
+    a.go = h->gs[h->cur];
+    if (h->form == DL_FORM_FP16) pops_from_host<__half, true><<<nblk(a.N, 256), 256, 0, h->stream>>>(a, d_f, d_g);
+    else pops_from_host<float, false><<<nblk(a.N, 256), 256, 0, h->stream>>>(a, d_f, d_g);
+    DL_CUDA(h, cudaGetLastError());
+    return DL_OK;
+}
+
+template <typename ST, bool RES, bool LES, bool FORCE>
+static int launch_fused(dl_handle* h, const FastArgs& a) {
+    static bool configured[64] = {false};
+    const int dev = h->device & 63;
+    const size_t sm = smem_bytes(LES);
+    if (!configured[dev]) {
+        DL_CUDA(h, cudaFuncSetAttribute(step_fused<ST, RES, LES, FORCE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)sm));
+        configured[dev] = true;
+    }
+    dim3 grid((a.nx + TX - 1) / TX, (a.ny + TY - 1) / TY, (a.nz + a.lz - 1) / a.lz);
+    DL_LAUNCH(h, true, (step_fused<ST, RES, LES, FORCE><<<grid, NT, sm, h->stream>>>(a)));
+    DL_CUDA(h, cudaGetLastError());
+    return DL_OK;
+}
+
+int fast_step(dl_handle* h) {
+    const int c = h->cur, n = 1 - c;
+    const long long step = h->step + 1;
+    if (h->force_mode == DL_FORCE_SPECTRAL) {
+        const float* m = h->mac32[c];
+        int rc = spectral_force_f32(h, m + h->N, m + 2 * h->N, m + 3 * h->N, h->force32, h->force32 + h->N,
+                                    h->force32 + 2 * h->N);
+        if (rc != DL_OK) return rc;
+    }
+    FastArgs a;
+    fill_fast(h, a);
+    a.mac = h->mac32[c];
+    a.maco = h->mac32[n];
+    a.f = h->fs[c];
+    a.g = h->gs[c];
+    a.fo = h->fs[n];
+    a.go = h->gs[n];
+    a.step = step;
+    double U[3] = {0.0, 0.0, 0.0};
+    if (step >= h->P.wall_start)
+        for (int k = 0; k < 3; ++k) U[k] = h->P.wall_u[k];
+    const int bot_src[5] = {6, 11, 12, 13, 10}, top_src[5] = {3, 14, 7, 8, 9};
+    for (int k = 0; k < 5; ++k) {
+        int j = bot_src[k];
+        a.wall_bot[k] = (float)(6.0 * h->lc.E[j] * ((-U[0]) * cx(j) + (-U[1]) * cy(j) + (-U[2]) * cz(j)));
+        j = top_src[k];
+        a.wall_top[k] = (float)(6.0 * h->lc.E[j] * (U[0] * cx(j) + U[1] * cy(j) + U[2] * cz(j)));
+    }
+    const bool les = h->P.les != 0;
+    const bool force = h->force_mode != DL_FORCE_NONE;
+    int rc;
+    if (h->form == DL_FORM_FP16) {
+        if (les) rc = force ? launch_fused<__half, true, true, true>(h, a) : launch_fused<__half, true, true, false>(h, a);
+        else rc = force ? launch_fused<__half, true, false, true>(h, a) : launch_fused<__half, true, false, false>(h, a);
+    } else {
+        if (les) rc = force ? launch_fused<float, false, true, true>(h, a) : launch_fused<float, false, true, false>(h, a);
+        else rc = force ? launch_fused<float, false, false, true>(h, a) : launch_fused<float, false, false, false>(h, a);
+    }
+    if (rc != DL_OK) return rc;
+    h->cur = n;
+    h->step = step;
+    return DL_OK;
+}
+
+}  // namespace dl
