@@ -150,6 +150,10 @@ def declare(lib: C.CDLL, prefix: str) -> None:
         lib.dl_profile.restype = C.c_int
         lib.dl_profile_read.argtypes = [h, C.POINTER(DLProfileStats)]
         lib.dl_profile_read.restype = C.c_int
+        lib.dl_set_option.argtypes = [h, C.c_char_p, C.c_int64]
+        lib.dl_set_option.restype = C.c_int
+        lib.dl_get_option.argtypes = [h, C.c_char_p, C.POINTER(C.c_int64)]
+        lib.dl_get_option.restype = C.c_int
     else:
         lib.orc_get_force.argtypes = [h, _dp, _dp, _dp]
         lib.orc_get_force.restype = C.c_int
@@ -183,4 +187,6 @@ HEADER_SYMBOLS = [
     "dl_last_error",
     "dl_profile",
     "dl_profile_read",
+    "dl_set_option",
+    "dl_get_option",
 ]

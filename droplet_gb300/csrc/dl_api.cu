@@ -216,6 +216,25 @@ int dl_profile_read(dl_handle* h, dl_profile_stats* out) {
     return DL_OK;
 }
 
+int dl_set_option(dl_handle* h, const char* key, int64_t value) {
+    if (!h || !key) return DL_ERR_ARG;
+    if (strcmp(key, "lz") == 0) {
+        if (value < 0 || value > h->nz) return set_error(h, DL_ERR_ARG, "lz=%lld outside 0..nz", (long long)value);
+        h->lz = value == 0 ? 16 : (int)value;
+        return DL_OK;
+    }
+    return set_error(h, DL_ERR_ARG, "unknown option '%s'", key);
+}
+
+int dl_get_option(dl_handle* h, const char* key, int64_t* value) {
+    if (!h || !key || !value) return DL_ERR_ARG;
+    if (strcmp(key, "lz") == 0) {
+        *value = h->lz;
+        return DL_OK;
+    }
+    return set_error(h, DL_ERR_ARG, "unknown option '%s'", key);
+}
+
 int dl_set_stream(dl_handle* h, void* stream) {
     if (!h) return DL_ERR_ARG;
     h->stream = (cudaStream_t)stream;
@@ -277,6 +296,13 @@ int dl_init_equilibrium(dl_handle* h) {
 int dl_set_force(dl_handle* h, int mode, const double* fx, const double* fy, const double* fz) {
     if (!h) return DL_ERR_ARG;
     const size_t N = h->N;
+    if (mode != DL_FORCE_NONE && mode != DL_FORCE_STATIC && mode != DL_FORCE_SPECTRAL) return DL_ERR_ARG;
+    if (mode == DL_FORCE_SPECTRAL && (h->P.kc < 2 || h->sp.K < 1))
+        return set_error(h, DL_ERR_ARG, "spectral forcing needs kc >= 2");
+    if (is_fast(h)) {
+        int rc = fast_prepare_force(h, mode);
+        if (rc != DL_OK) return rc;
+    }
     if (mode == DL_FORCE_STATIC) {
         if (!fx || !fy || !fz) return DL_ERR_ARG;
         const double* src[3] = {fx, fy, fz};
@@ -295,9 +321,9 @@ int dl_set_force(dl_handle* h, int mode, const double* fx, const double* fy, con
                                            h->stream));
         }
     } else if (mode == DL_FORCE_NONE || mode == DL_FORCE_SPECTRAL) {
-        if (mode == DL_FORCE_SPECTRAL && (h->P.kc < 2 || h->sp.K < 1))
-            return set_error(h, DL_ERR_ARG, "spectral forcing needs kc >= 2");
-        if (is_fast(h)) DL_CUDA(h, cudaMemsetAsync(h->force32, 0, 3 * N * sizeof(float), h->stream));
+        if (is_fast(h)) {
+            if (h->force32) DL_CUDA(h, cudaMemsetAsync(h->force32, 0, 3 * N * sizeof(float), h->stream));
+        }
         else DL_CUDA(h, cudaMemsetAsync(h->force64, 0, 3 * N * sizeof(double), h->stream));
     } else {
         return DL_ERR_ARG;

@@ -16,10 +16,12 @@ __device__ __forceinline__ int wrapi(int v, int n) { return v < 0 ? v + n : (v >
 // case is resolved by an exact ordered scan in the last block.
 // phi values are phi_off + phi_new[k] evaluated in T (the FP32 forms store
 // phi - phi1 and pass phi_off = phi1).
+// nblk is the number of blocks that reduce into st (the whole grid for one
+// domain). Returns true in the last block (after it has finalised).
 template <typename T>
-__device__ void minmax_block_and_finalize(DevState* st, double vmin, double vmax, const T* phi_new, T phi_off,
+__device__ bool minmax_block_and_finalize(DevState* st, double vmin, double vmax, const T* phi_new, T phi_off,
                                           long long N, double phi1, double phi2, bool nan_seen,
-                                          long long step) {
+                                          long long step, unsigned nblk) {
     __shared__ long long smin[32], smax[32];
     __shared__ int s_last;
     __shared__ int s_nan;
@@ -55,10 +57,10 @@ __device__ void minmax_block_and_finalize(DevState* st, double vmin, double vmax
         }
         __threadfence();
         unsigned t = atomicAdd(&st->blocks_done, 1u);
-        s_last = (t == gridDim.x * gridDim.y * gridDim.z - 1);
+        s_last = (t == nblk - 1);
     }
     __syncthreads();
-    if (!s_last) return;
+    if (!s_last) return false;
     __threadfence();
     // ---- last block: finalise ----
     __shared__ double s_mn, s_mx;
@@ -139,6 +141,7 @@ __device__ void minmax_block_and_finalize(DevState* st, double vmin, double vmax
         __threadfence();
         st->blocks_done = 0u;
     }
+    return true;
 }
 
 }  // namespace dl

@@ -88,6 +88,18 @@ struct SpectralPlan {
     float* d_twxf;    // FP32 copy of d_twx
 };
 
+// In-kernel band forcing of the FP32 / FP16 forms.
+struct FastSpectral {
+    int nm;              // number of band modes (0: not used)
+    int par;             // which of d_fh the next step reads
+    int dirty;           // the coefficients must be recomputed from the current u
+    int4* d_modes;       // kx, ky, kz, weight
+    int* d_kxoff;        // first mode of each kx
+    float2* d_tw[3];     // e^{i 2 pi m / n} for x, y, z
+    float2* d_fh[2];     // [3][nm] synthesis coefficients
+    double* d_acc;       // [3][nm][2] projection accumulators
+};
+
 }  // namespace dl
 
 struct dl_handle {
@@ -123,6 +135,7 @@ struct dl_handle {
     int lz;                  // z planes per block of the fused kernel
 
     dl::SpectralPlan sp;
+    dl::FastSpectral fsp;
     double* d_diag;          // diagnostics partial sums
     int diag_blocks;
 
@@ -159,6 +172,8 @@ int fast_init_equilibrium(dl_handle* h);
 int fast_get_populations(dl_handle* h, double* d_f, double* d_g);
 int fast_set_populations(dl_handle* h, const double* d_f, const double* d_g);
 int fast_step(dl_handle* h);
+int fast_prepare_force(dl_handle* h, int mode);
+int spectral_project_f32(dl_handle* h, const float* d_u1, const float* d_u2, const float* d_u3);
 // transposes (layout.cu)
 int soa_to_aos(dl_handle* h, const double* d_soa, double* d_aos);
 int aos_to_soa(dl_handle* h, const double* d_aos, double* d_soa);

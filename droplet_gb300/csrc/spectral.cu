@@ -408,6 +408,21 @@ int spectral_force_fp64(dl_handle* h, const double* u1, const double* u2, const 
     return DL_OK;
 }
 
+// forward part only: sp.d_uh = band coefficients u_hat / N of an FP32 u
+int spectral_project_f32(dl_handle* h, const float* u1, const float* u2, const float* u3) {
+    SpArgs a;
+    fill_sp(h, a);
+    const int NK = 2 * a.K + 1;
+    cudaStream_t s = h->stream;
+    const long long rows = (long long)h->ny * h->nz;
+    DL_LAUNCH(h, false, sp_xstage_f32<<<nb(rows * 32, 256), 256, 0, s>>>(u1, u2, u3, a.a1, h->nx, h->ny, h->nz, a.K,
+                                                                        h->sp.d_twxf));
+    DL_LAUNCH(h, false, sp_ystage<<<nb(3LL * NK * NK * h->nz, 128), 128, 0, s>>>(a));
+    DL_LAUNCH(h, false, sp_zstage<<<nb(3LL * NK * NK * (a.K + 1), 64), 64, 0, s>>>(a));
+    DL_CUDA(h, cudaGetLastError());
+    return DL_OK;
+}
+
 int spectral_force_f32(dl_handle* h, const float* u1, const float* u2, const float* u3, float* fx, float* fy,
                        float* fz) {
     SpArgs a;

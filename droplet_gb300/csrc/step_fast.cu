@@ -4,8 +4,8 @@
 //   FP32 form: as deviations from the bulk equilibrium at phi = phi1, p = 1/3,
 //              u = 0:  df_i = f_i - (H_i phi1 + F_i p0(phi1)),  dg_i = g_i - E_i;
 //   FP16 form: as FP16 residuals against the local part of the equilibrium,
-//              r_i = f_i - (H_i phi + F_i p0(phi) + 3 E_i phi c_i.u) - f_ref,
-//              s_i = g_i - E_i (3p + 3 c_i.u + 4.5 (c_i.u)^2 - 1.5 u^2),
+//              r_i = df_i - (H_i dphi + F_i dp0(phi) + 3 E_i phi c_i.u),
+//              s_i = dg_i - E_i (3 dp + 3 c_i.u + 4.5 (c_i.u)^2 - 1.5 u^2),
 //              rebuilt from the FP32 moments of the same site when read.
 // The macroscopic fields are FP32: dphi = phi - phi1, u, dp = p - 1/3.
 //
@@ -24,19 +24,35 @@
 //     applies the moving-wall bounce-back, takes the moments, stores
 //     populations and fields, and reduces phi min/max; the last block turns
 //     the reduction into the next step's tau_g range.
+// Body force (FMODE):
+//   F_NONE     no force;
+//   F_ARRAY    Fx, Fy, Fz read from HBM at the record sites (static force, or
+//              the spectral force for kc > 3 computed by separate launches);
+//   F_SPECTRAL the band forcing of program/lbm_drop_iht_xy.f90:722-842 done
+//              inside the step: the force at each record site is synthesised
+//              from the band coefficients through a per-plane table in shared
+//              memory, and the band projection of the new u is accumulated in
+//              the epilogue (a warp-level separable DFT along x, one set of
+//              FP64 atomics per block); the last block turns it into the
+//              next step's coefficients. No force array touches HBM.
 #include "dl_internal.cuh"
 #include "dl_device.cuh"
 
 #include <cuda_fp16.h>
 #include <math.h>
 #include <string.h>
+#include <vector>
 
 namespace dl {
 
-constexpr int TX = 32, TY = 8, NT = TX * TY;
+constexpr int TX = 32, TY = 8, NT = TX * TY, NWARP = NT / 32;
 constexpr int EX1 = TX + 2, EY1 = TY + 2, P1 = EX1 * EY1;  // record plane (1-cell halo)
 constexpr int EX2 = TX + 4, EY2 = TY + 4, P2 = EX2 * EY2;  // staging plane (2-cell halo)
 enum { R_DPHI, R_U1, R_U2, R_U3, R_DA, R_S, R_OMG, R_GX, R_GY, R_GZ, R_GSQ, R_DP0, R_FX, R_FY, R_FZ, NR };
+enum { F_NONE = 0, F_ARRAY = 1, F_SPECTRAL = 2 };
+constexpr int SK = 2;                 // in-kernel spectral forcing: |k_x| <= 2 (kc <= 3)
+constexpr int SNK = 2 * SK + 1;
+constexpr int SMAXM = 64;             // at most 64 band modes (two per lane)
 
 struct FastArgs {
     int nx, ny, nz, lz;
@@ -47,13 +63,24 @@ struct FastArgs {
     const void* g;
     void* fo;
     void* go;
-    const float* force;  // [3][N]
+    const float* force;  // [3][N] (F_ARRAY)
     DevState* st;
     float phi1, phi2, omf, kf, kf6, kg, T, a, b, omb1, nu1, dnu, csd, anu23, inv_ds, inv_lap, inv_grad;
     float fref[Q];   // bulk equilibrium of f (FP32 form offsets)
     float wall_bot[5], wall_top[5];
     int walls, visc_fixed;
     long long step;
+    // in-kernel spectral forcing (F_SPECTRAL)
+    int nm;               // number of band modes (half spectrum kz >= 0)
+    const int4* modes;    // kx, ky, kz, weight; sorted by kx
+    const int* kx_off;    // [SNK + 1] first mode of each kx = -2..2
+    const float2* fh;     // [3][nm] w * (0.5 eps / E) * u_hat, used by this step
+    float2* fh_next;      // [3][nm] written by the last block
+    double* acc;          // [3][nm][2] sum over sites of u e^{-i k.x} of the new u
+    const float2* twx;    // e^{+i 2 pi m / n}
+    const float2* twy;
+    const float2* twz;
+    double half_eps, invN;
 };
 
 __device__ __forceinline__ int pmod(int v, int n) {
@@ -66,7 +93,7 @@ __device__ __forceinline__ constexpr float Ew(int i) { return i == 0 ? 2.0f / 9.
 __device__ __forceinline__ constexpr float Fw(int i) { return i == 0 ? -7.0f / 3.0f : (i <= 6 ? 1.0f / 3.0f : 1.0f / 24.0f); }
 __device__ __forceinline__ constexpr float c2w(int i) { return i == 0 ? 0.f : (i <= 6 ? 1.f : 3.f); }
 
-// c_i . (a, b, c) with the zero terms dropped; explicit roundings so that the
+// c_i . (p, q, r) with the zero terms dropped; explicit roundings so that the
 // same inputs give the same bits wherever it is inlined
 __device__ __forceinline__ float cdot3(int i, float p, float q, float r) {
     float s = 0.f;
@@ -210,15 +237,58 @@ __device__ __forceinline__ void collide_dir(const FastArgs& a, int i, const Rec&
     if (FORCE && i != 0) go += 3.f * E * cdot3(i, r.Fx, r.Fy, r.Fz);
 }
 
+// last block: band energy E = sum_m 0.5 w_m |u_hat_m|^2, u_hat = acc / N, and
+// the coefficients w_m (0.5 eps / E) u_hat_m of the next step; zeroes acc
+__device__ void spectral_finalize(const FastArgs& a) {
+    __shared__ double s_e[NWARP];
+    __shared__ double s_coef;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    double e = 0.0;
+    for (int m = tid; m < a.nm; m += blockDim.x) {
+        double s = 0.0;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const double re = __ldcg(a.acc + 2 * (c * a.nm + m)) * a.invN;
+            const double im = __ldcg(a.acc + 2 * (c * a.nm + m) + 1) * a.invN;
+            s += re * re + im * im;
+        }
+        e += 0.5 * (double)a.modes[m].w * s;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
+    if (lane == 0) s_e[warp] = e;
+    __syncthreads();
+    if (tid == 0) {
+        double E = 0.0;
+        for (int w = 0; w < NWARP; ++w) E += s_e[w];
+        s_coef = a.half_eps / E;
+        a.st->sp_energy = E;
+        a.st->sp_coef = s_coef;
+    }
+    __syncthreads();
+    const double coef = s_coef;
+    for (int t = tid; t < 3 * a.nm; t += blockDim.x) {
+        const int m = t % a.nm;
+        const double k = coef * a.invN * (double)a.modes[m].w;
+        double* p = a.acc + 2 * t;
+        a.fh_next[t] = make_float2((float)(k * __ldcg(p)), (float)(k * __ldcg(p + 1)));
+        p[0] = 0.0;
+        p[1] = 0.0;
+    }
+}
+
 // ---- the fused step kernel ---------------------------------------------------
-template <typename ST, bool RES, bool LES, bool FORCE>
+template <typename ST, bool RES, bool LES, int FMODE>
 __global__ void __launch_bounds__(NT, 2) step_fused(const FastArgs a) {
+    constexpr bool FORCE = FMODE != F_NONE;
+    constexpr bool SPEC = FMODE == F_SPECTRAL;
     extern __shared__ float smem[];
     float* s_phi = smem;                            // [3][P2]
     float* s_u = s_phi + 3 * P2;                    // [3][3][P2] (LES)
     float* s_rec = s_u + (LES ? 9 * P2 : 0);        // [3][NR][P1]
+    float2* s_C = (float2*)(s_rec + 3 * NR * P1);   // [3][SNK][EY1] (SPEC)
     const int tid = threadIdx.x;
-    const int tx = tid % TX, ty = tid / TX;
+    const int tx = tid % TX, ty = tid / TX, lane = tid & 31;
     const int nx = a.nx, ny = a.ny, nz = a.nz;
     const long long N = a.N;
     const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * a.lz;
@@ -247,6 +317,27 @@ __global__ void __launch_bounds__(NT, 2) step_fused(const FastArgs a) {
         }
     };
 
+    // force synthesis table of plane zr: C[c][kx][row] = sum over the modes
+    // with this kx of w f_hat e^{i (ky y + kz z)}
+    auto ctable = [&](int zr) {
+        const int zw = pmod(zr, nz);
+        for (int t = tid; t < 3 * SNK * EY1; t += NT) {
+            const int yy = t % EY1, r = t / EY1, kxi = r % SNK, c = r / SNK;
+            const int yg = pmod(y0 - 1 + yy, ny);
+            float re = 0.f, im = 0.f;
+            for (int m = a.kx_off[kxi]; m < a.kx_off[kxi + 1]; ++m) {
+                const int4 md = a.modes[m];
+                const float2 ey = a.twy[pmod(md.y * yg, ny)];
+                const float2 ez = a.twz[pmod(md.z * zw, nz)];
+                const float pr = ey.x * ez.x - ey.y * ez.y, pi = ey.x * ez.y + ey.y * ez.x;
+                const float2 fv = a.fh[c * a.nm + m];
+                re += fv.x * pr - fv.y * pi;
+                im += fv.x * pi + fv.y * pr;
+            }
+            s_C[t] = make_float2(re, im);
+        }
+    };
+
     auto records = [&](int zr) {
         const int sc = (zr + 3) % 3, sm1 = (zr + 2) % 3, sp1 = (zr + 4) % 3;
         float* R = s_rec + ((zr + 3) % 3) * NR * P1;
@@ -260,7 +351,8 @@ __global__ void __launch_bounds__(NT, 2) step_fused(const FastArgs a) {
                 const int sl = cz(i) == 0 ? sc : (cz(i) > 0 ? sp1 : sm1);
                 v[i] = s_phi[sl * P2 + c2 + cy(i) * EX2 + cx(i)];
             }
-            const long long s = pmod(x0 - 1 + ex, nx) + (long long)nx * (pmod(y0 - 1 + ey, ny) + (long long)ny * zw);
+            const int xg = pmod(x0 - 1 + ex, nx);
+            const long long s = xg + (long long)nx * (pmod(y0 - 1 + ey, ny) + (long long)ny * zw);
             float u1, u2, u3;
             float w[3][Q];
             if (LES) {
@@ -293,10 +385,24 @@ __global__ void __launch_bounds__(NT, 2) step_fused(const FastArgs a) {
             R[R_GZ * P1 + k] = r.gz;
             R[R_GSQ * P1 + k] = r.gsq;
             if (RES) R[R_DP0 * P1 + k] = r.dp0;
-            if (FORCE) {
+            if (FMODE == F_ARRAY) {
                 R[R_FX * P1 + k] = __ldg(a.force + s);
                 R[R_FY * P1 + k] = __ldg(a.force + N + s);
                 R[R_FZ * P1 + k] = __ldg(a.force + 2 * N + s);
+            } else if (SPEC) {
+                float F[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+                for (int kxi = 0; kxi < SNK; ++kxi) {
+                    const float2 ex_ = a.twx[pmod((kxi - SK) * xg, nx)];
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        const float2 cv = s_C[(c * SNK + kxi) * EY1 + ey];
+                        F[c] += cv.x * ex_.x - cv.y * ex_.y;
+                    }
+                }
+                R[R_FX * P1 + k] = F[0];
+                R[R_FY * P1 + k] = F[1];
+                R[R_FZ * P1 + k] = F[2];
             }
         }
     };
@@ -305,10 +411,12 @@ __global__ void __launch_bounds__(NT, 2) step_fused(const FastArgs a) {
     stage(z0 - 2);
     stage(z0 - 1);
     stage(z0);
+    if (SPEC) ctable(z0 - 1);
     __syncthreads();
     records(z0 - 1);
     __syncthreads();
     stage(z0 + 1);
+    if (SPEC) ctable(z0);
     __syncthreads();
     records(z0);
     __syncthreads();
@@ -317,6 +425,12 @@ __global__ void __launch_bounds__(NT, 2) step_fused(const FastArgs a) {
     const bool act = gxd < nx && gyd < ny;
     double bmin = INFINITY, bmax = -INFINITY;
     bool bad = false;
+    // band projection of the new u: lane l accumulates modes l and l + 32
+    float pacc[2][3][2];
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) pacc[j][c][0] = pacc[j][c][1] = 0.f;
 
     for (int z = z0; z < z1; ++z) {
         // populations of the destination plane, pulled from x - c_i
@@ -331,9 +445,11 @@ __global__ void __launch_bounds__(NT, 2) step_fused(const FastArgs a) {
             }
         }
         stage(z + 2);
+        if (SPEC) ctable(z + 1);
         __syncthreads();
         records(z + 1);
         __syncthreads();
+        float u1n = 0.f, u2n = 0.f, u3n = 0.f;
         if (act) {
             float fo[Q], go[Q];
 #pragma unroll
@@ -380,7 +496,7 @@ __global__ void __launch_bounds__(NT, 2) step_fused(const FastArgs a) {
                 }
             }
             // moments (physics, program/lbm_drop_xy.f90:541-552)
-            float dphin = 0.f, dpn = 0.f, u1n = 0.f, u2n = 0.f, u3n = 0.f;
+            float dphin = 0.f, dpn = 0.f;
 #pragma unroll
             for (int i = 0; i < Q; ++i) {
                 dphin += fo[i];
@@ -423,9 +539,84 @@ __global__ void __launch_bounds__(NT, 2) step_fused(const FastArgs a) {
             }
             bad |= !(isfinite(dphin) && isfinite(dpn) && isfinite(u1n) && isfinite(u2n) && isfinite(u3n));
         }
+        if (SPEC) {
+            // x stage of the band projection over this warp's row (one y, one z)
+            float sr[3][SK + 1], si[3][SK + 1];
+#pragma unroll
+            for (int k = 0; k <= SK; ++k) {
+                const float2 e = a.twx[pmod(k * gxd, nx)];
+                const float u[3] = {u1n, u2n, u3n};  // zero for inactive lanes
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    sr[c][k] = u[c] * e.x;
+                    si[c][k] = -u[c] * e.y;
+                }
+            }
+#pragma unroll
+            for (int k = 0; k <= SK; ++k)
+#pragma unroll
+                for (int c = 0; c < 3; ++c)
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) {
+                        sr[c][k] += __shfl_xor_sync(0xffffffffu, sr[c][k], o);
+                        si[c][k] += __shfl_xor_sync(0xffffffffu, si[c][k], o);
+                    }
+            const int yw = pmod(gyd, ny);
+#pragma unroll
+            for (int j = 0; j < 2; ++j) {
+                const int m = lane + 32 * j;
+                if (m < a.nm) {
+                    const int4 md = a.modes[m];
+                    const float2 ey = a.twy[pmod(md.y * yw, ny)];
+                    const float2 ez = a.twz[pmod(md.z * z, nz)];
+                    // e^{-i (ky y + kz z)}
+                    const float pr = ey.x * ez.x - ey.y * ez.y, pi = -(ey.x * ez.y + ey.y * ez.x);
+                    const int ak = md.x < 0 ? -md.x : md.x;
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        float xr = 0.f, xi = 0.f;
+#pragma unroll
+                        for (int k = 0; k <= SK; ++k)
+                            if (k == ak) {
+                                xr = sr[c][k];
+                                xi = si[c][k];
+                            }
+                        if (md.x < 0) xi = -xi;
+                        pacc[j][c][0] += xr * pr - xi * pi;
+                        pacc[j][c][1] += xr * pi + xi * pr;
+                    }
+                }
+            }
+        }
     }
-    minmax_block_and_finalize<float>(a.st, bmin, bmax, a.maco, a.phi1, N, (double)a.phi1, (double)a.phi2, bad,
-                                     a.step);
+    if (SPEC) {
+        // block sum of the warps' projections, then one FP64 atomic per value
+        __syncthreads();
+        float* red = s_rec;  // [NWARP][3][SMAXM][2], the record ring is free now
+        const int warp = tid >> 5;
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            const int m = lane + 32 * j;
+            if (m < a.nm)
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    red[((warp * 3 + c) * SMAXM + m) * 2 + 0] = pacc[j][c][0];
+                    red[((warp * 3 + c) * SMAXM + m) * 2 + 1] = pacc[j][c][1];
+                }
+        }
+        __syncthreads();
+        for (int t = tid; t < 3 * a.nm * 2; t += NT) {
+            const int part = t & 1, cm = t >> 1, c = cm / a.nm, m = cm % a.nm;
+            float s = 0.f;
+            for (int w = 0; w < NWARP; ++w) s += red[((w * 3 + c) * SMAXM + m) * 2 + part];
+            atomicAdd(a.acc + 2 * (c * a.nm + m) + part, (double)s);
+        }
+        __threadfence();  // the last block reads acc after every block's ticket
+    }
+    const unsigned nblk = gridDim.x * gridDim.y * gridDim.z;
+    const bool last = minmax_block_and_finalize<float>(a.st, bmin, bmax, a.maco, a.phi1, N, (double)a.phi1,
+                                                       (double)a.phi2, bad, a.step, nblk);
+    if (SPEC && last) spectral_finalize(a);
 }
 
 // ---- initial populations f = feq, g = geq at every site (ini :244-251) -------
@@ -557,8 +748,52 @@ __global__ void pops_from_host(const FastArgs a, const double* __restrict__ fa, 
     }
 }
 
+// band coefficients of the current u from the separable DFT stages
+// (u_hat = uh[c][kx][ky][kz], already / N): E, coefficient and fh for the
+// in-kernel synthesis; one block
+__global__ void sp_fhat_from_uh(const double* __restrict__ uh, int K, const int4* __restrict__ modes, int nm,
+                                double half_eps, float2* __restrict__ fh, DevState* st) {
+    __shared__ double s_e[8];
+    __shared__ double s_coef;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int NK = 2 * K + 1;
+    double e = 0.0;
+    for (int m = tid; m < nm; m += blockDim.x) {
+        const int4 md = modes[m];
+        double s = 0.0;
+        for (int c = 0; c < 3; ++c) {
+            const double* v = uh + 2 * ((((long long)c * NK + (md.x + K)) * NK + (md.y + K)) * (K + 1) + md.z);
+            s += v[0] * v[0] + v[1] * v[1];
+        }
+        e += 0.5 * (double)md.w * s;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
+    if (lane == 0) s_e[warp] = e;
+    __syncthreads();
+    if (tid == 0) {
+        double E = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) E += s_e[w];
+        s_coef = half_eps / E;
+        st->sp_energy = E;
+        st->sp_coef = s_coef;
+    }
+    __syncthreads();
+    for (int t = tid; t < 3 * nm; t += blockDim.x) {
+        const int c = t / nm, m = t % nm;
+        const int4 md = modes[m];
+        const double* v = uh + 2 * ((((long long)c * NK + (md.x + K)) * NK + (md.y + K)) * (K + 1) + md.z);
+        const double k = s_coef * (double)md.w;
+        fh[t] = make_float2((float)(k * v[0]), (float)(k * v[1]));
+    }
+}
+
 // ---- host side ---------------------------------------------------------------------
-static size_t smem_bytes(bool les) { return sizeof(float) * (3 * P2 + (les ? 9 * P2 : 0) + 3 * NR * P1); }
+static size_t smem_bytes(bool les, int fmode) {
+    size_t n = 3 * P2 + (les ? 9 * P2 : 0) + 3 * NR * P1;
+    if (fmode == F_SPECTRAL) n += 2 * 3 * SNK * EY1;
+    return sizeof(float) * n;
+}
 
 static void fill_fast(dl_handle* h, FastArgs& a) {
     const dl_params& P = h->P;
@@ -591,9 +826,74 @@ static void fill_fast(dl_handle* h, FastArgs& a) {
     a.walls = P.walls ? 1 : 0;
     a.visc_fixed = (P.visc_mode == DL_VISC_FIXED) ? 1 : 0;
     a.force = h->force32;
+    const FastSpectral& fs = h->fsp;
+    a.nm = fs.nm;
+    a.modes = fs.d_modes;
+    a.kx_off = fs.d_kxoff;
+    a.twx = fs.d_tw[0];
+    a.twy = fs.d_tw[1];
+    a.twz = fs.d_tw[2];
+    a.acc = fs.d_acc;
+    a.fh = fs.d_fh[fs.par];
+    a.fh_next = fs.d_fh[1 - fs.par];
+    a.half_eps = 0.5 * P.eps;
+    a.invN = 1.0 / ((double)h->nx * (double)h->ny * (double)h->nz);
 }
 
 static inline unsigned nblk(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+
+// band mode list (half spectrum kz >= 0, 1 <= |k|^2 < kc^2) sorted by kx, and
+// e^{i 2 pi m / n} tables, for the in-kernel forcing
+static int fast_spectral_alloc(dl_handle* h) {
+    FastSpectral& fs = h->fsp;
+    memset(&fs, 0, sizeof(fs));
+    const int K = h->P.kc - 1;
+    if (K < 1 || K > SK) return DL_OK;  // kc > 3: separate forcing launches
+    std::vector<int4> modes;
+    std::vector<int> off(SNK + 1, 0);
+    for (int kx = -SK; kx <= SK; ++kx) {
+        off[kx + SK] = (int)modes.size();
+        for (int kz = 0; kz <= K; ++kz)
+            for (int ky = -K; ky <= K; ++ky) {
+                const int kk = kx * kx + ky * ky + kz * kz;
+                if (kk >= 1 && kk < h->P.kc * h->P.kc) modes.push_back(make_int4(kx, ky, kz, kz == 0 ? 1 : 2));
+            }
+    }
+    off[SNK] = (int)modes.size();
+    if ((int)modes.size() > SMAXM) return DL_OK;
+    fs.nm = (int)modes.size();
+    DL_CUDA(h, cudaMalloc(&fs.d_modes, sizeof(int4) * fs.nm));
+    DL_CUDA(h, cudaMemcpy(fs.d_modes, modes.data(), sizeof(int4) * fs.nm, cudaMemcpyHostToDevice));
+    DL_CUDA(h, cudaMalloc(&fs.d_kxoff, sizeof(int) * (SNK + 1)));
+    DL_CUDA(h, cudaMemcpy(fs.d_kxoff, off.data(), sizeof(int) * (SNK + 1), cudaMemcpyHostToDevice));
+    const int ns[3] = {h->nx, h->ny, h->nz};
+    const double pi = acos(-1.0);
+    for (int d = 0; d < 3; ++d) {
+        std::vector<float2> t(ns[d]);
+        for (int m = 0; m < ns[d]; ++m)
+            t[m] = make_float2((float)cos(2.0 * pi * m / ns[d]), (float)sin(2.0 * pi * m / ns[d]));
+        DL_CUDA(h, cudaMalloc(&fs.d_tw[d], sizeof(float2) * ns[d]));
+        DL_CUDA(h, cudaMemcpy(fs.d_tw[d], t.data(), sizeof(float2) * ns[d], cudaMemcpyHostToDevice));
+    }
+    for (int k = 0; k < 2; ++k) {
+        DL_CUDA(h, cudaMalloc(&fs.d_fh[k], sizeof(float2) * 3 * fs.nm));
+        DL_CUDA(h, cudaMemset(fs.d_fh[k], 0, sizeof(float2) * 3 * fs.nm));
+    }
+    DL_CUDA(h, cudaMalloc(&fs.d_acc, sizeof(double) * 2 * 3 * fs.nm));
+    DL_CUDA(h, cudaMemset(fs.d_acc, 0, sizeof(double) * 2 * 3 * fs.nm));
+    fs.dirty = 1;
+    return DL_OK;
+}
+
+static void fast_spectral_free(dl_handle* h) {
+    FastSpectral& fs = h->fsp;
+    cudaFree(fs.d_modes);
+    cudaFree(fs.d_kxoff);
+    for (int d = 0; d < 3; ++d) cudaFree(fs.d_tw[d]);
+    for (int k = 0; k < 2; ++k) cudaFree(fs.d_fh[k]);
+    cudaFree(fs.d_acc);
+    memset(&fs, 0, sizeof(fs));
+}
 
 int fast_alloc(dl_handle* h) {
     const size_t N = h->N;
@@ -606,9 +906,21 @@ int fast_alloc(dl_handle* h) {
         DL_CUDA(h, cudaMemsetAsync(h->gs[k], 0, es * Q * N, h->stream));
         DL_CUDA(h, cudaMemsetAsync(h->mac32[k], 0, sizeof(float) * 5 * N, h->stream));
     }
-    DL_CUDA(h, cudaMalloc(&h->force32, sizeof(float) * 3 * N));
-    DL_CUDA(h, cudaMemsetAsync(h->force32, 0, sizeof(float) * 3 * N, h->stream));
     if (h->lz <= 0) h->lz = 16;
+    return fast_spectral_alloc(h);
+}
+
+// the force arrays are only needed for a static force or kc > 3
+static int ensure_force32(dl_handle* h) {
+    if (h->force32) return DL_OK;
+    DL_CUDA(h, cudaMalloc(&h->force32, sizeof(float) * 3 * h->N));
+    DL_CUDA(h, cudaMemsetAsync(h->force32, 0, sizeof(float) * 3 * h->N, h->stream));
+    return DL_OK;
+}
+
+int fast_prepare_force(dl_handle* h, int mode) {
+    if (mode == DL_FORCE_STATIC || (mode == DL_FORCE_SPECTRAL && h->fsp.nm == 0)) return ensure_force32(h);
+    if (mode == DL_FORCE_SPECTRAL) h->fsp.dirty = 1;
     return DL_OK;
 }
 
@@ -622,11 +934,13 @@ void fast_free(dl_handle* h) {
     }
     cudaFree(h->force32);
     h->force32 = nullptr;
+    fast_spectral_free(h);
 }
 
 int fast_set_fields(dl_handle* h, const double* d_fields) {
     fields_to_fast<<<nblk(h->N, 256), 256, 0, h->stream>>>(d_fields, h->mac32[h->cur], (long long)h->N, h->P.phi1);
     DL_CUDA(h, cudaGetLastError());
+    h->fsp.dirty = 1;
     return DL_OK;
 }
 
@@ -645,6 +959,7 @@ int fast_init_equilibrium(dl_handle* h) {
     if (h->form == DL_FORM_FP16) DL_LAUNCH(h, false, (init_fast<__half, true><<<nblk(a.N, 256), 256, 0, h->stream>>>(a)));
     else DL_LAUNCH(h, false, (init_fast<float, false><<<nblk(a.N, 256), 256, 0, h->stream>>>(a)));
     DL_CUDA(h, cudaGetLastError());
+    h->fsp.dirty = 1;
     return DL_OK;
 }
 
@@ -669,33 +984,72 @@ int fast_set_populations(dl_handle* h, const double* d_f, const double* d_g) {
     if (h->form == DL_FORM_FP16) pops_from_host<__half, true><<<nblk(a.N, 256), 256, 0, h->stream>>>(a, d_f, d_g);
     else pops_from_host<float, false><<<nblk(a.N, 256), 256, 0, h->stream>>>(a, d_f, d_g);
     DL_CUDA(h, cudaGetLastError());
+    h->fsp.dirty = 1;
     return DL_OK;
 }
 
-template <typename ST, bool RES, bool LES, bool FORCE>
+// band coefficients from the current u (first step after new fields)
+static int fast_spectral_project(dl_handle* h) {
+    const float* m = h->mac32[h->cur];
+    int rc = spectral_project_f32(h, m + h->N, m + 2 * h->N, m + 3 * h->N);
+    if (rc != DL_OK) return rc;
+    FastSpectral& fs = h->fsp;
+    DL_LAUNCH(h, false, (sp_fhat_from_uh<<<1, 256, 0, h->stream>>>(h->sp.d_uh, h->sp.K, fs.d_modes, fs.nm,
+                                                                  0.5 * h->P.eps, fs.d_fh[fs.par], h->d_state)));
+    DL_CUDA(h, cudaMemsetAsync(fs.d_acc, 0, sizeof(double) * 2 * 3 * fs.nm, h->stream));
+    DL_CUDA(h, cudaGetLastError());
+    fs.dirty = 0;
+    return DL_OK;
+}
+
+template <typename ST, bool RES, bool LES, int FMODE>
 static int launch_fused(dl_handle* h, const FastArgs& a) {
     static bool configured[64] = {false};
     const int dev = h->device & 63;
-    const size_t sm = smem_bytes(LES);
+    const size_t sm = smem_bytes(LES, FMODE);
     if (!configured[dev]) {
-        DL_CUDA(h, cudaFuncSetAttribute(step_fused<ST, RES, LES, FORCE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        DL_CUDA(h, cudaFuncSetAttribute(step_fused<ST, RES, LES, FMODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)sm));
         configured[dev] = true;
     }
     dim3 grid((a.nx + TX - 1) / TX, (a.ny + TY - 1) / TY, (a.nz + a.lz - 1) / a.lz);
-    DL_LAUNCH(h, true, (step_fused<ST, RES, LES, FORCE><<<grid, NT, sm, h->stream>>>(a)));
+    DL_LAUNCH(h, true, (step_fused<ST, RES, LES, FMODE><<<grid, NT, sm, h->stream>>>(a)));
     DL_CUDA(h, cudaGetLastError());
     return DL_OK;
+}
+
+template <typename ST, bool RES>
+static int dispatch(dl_handle* h, const FastArgs& a, bool les, int fmode) {
+    if (les) {
+        if (fmode == F_SPECTRAL) return launch_fused<ST, RES, true, F_SPECTRAL>(h, a);
+        if (fmode == F_ARRAY) return launch_fused<ST, RES, true, F_ARRAY>(h, a);
+        return launch_fused<ST, RES, true, F_NONE>(h, a);
+    }
+    if (fmode == F_SPECTRAL) return launch_fused<ST, RES, false, F_SPECTRAL>(h, a);
+    if (fmode == F_ARRAY) return launch_fused<ST, RES, false, F_ARRAY>(h, a);
+    return launch_fused<ST, RES, false, F_NONE>(h, a);
 }
 
 int fast_step(dl_handle* h) {
     const int c = h->cur, n = 1 - c;
     const long long step = h->step + 1;
-    if (h->force_mode == DL_FORCE_SPECTRAL) {
-        const float* m = h->mac32[c];
-        int rc = spectral_force_f32(h, m + h->N, m + 2 * h->N, m + 3 * h->N, h->force32, h->force32 + h->N,
-                                    h->force32 + 2 * h->N);
-        if (rc != DL_OK) return rc;
+    int fmode = F_NONE;
+    if (h->force_mode == DL_FORCE_STATIC) {
+        fmode = F_ARRAY;
+    } else if (h->force_mode == DL_FORCE_SPECTRAL) {
+        if (h->fsp.nm > 0) {
+            fmode = F_SPECTRAL;
+            if (h->fsp.dirty) {
+                int rc = fast_spectral_project(h);
+                if (rc != DL_OK) return rc;
+            }
+        } else {
+            fmode = F_ARRAY;
+            const float* m = h->mac32[c];
+            int rc = spectral_force_f32(h, m + h->N, m + 2 * h->N, m + 3 * h->N, h->force32, h->force32 + h->N,
+                                        h->force32 + 2 * h->N);
+            if (rc != DL_OK) return rc;
+        }
     }
     FastArgs a;
     fill_fast(h, a);
@@ -717,16 +1071,10 @@ int fast_step(dl_handle* h) {
         a.wall_top[k] = (float)(6.0 * h->lc.E[j] * (U[0] * cx(j) + U[1] * cy(j) + U[2] * cz(j)));
     }
     const bool les = h->P.les != 0;
-    const bool force = h->force_mode != DL_FORCE_NONE;
-    int rc;
-    if (h->form == DL_FORM_FP16) {
-        if (les) rc = force ? launch_fused<__half, true, true, true>(h, a) : launch_fused<__half, true, true, false>(h, a);
-        else rc = force ? launch_fused<__half, true, false, true>(h, a) : launch_fused<__half, true, false, false>(h, a);
-    } else {
-        if (les) rc = force ? launch_fused<float, false, true, true>(h, a) : launch_fused<float, false, true, false>(h, a);
-        else rc = force ? launch_fused<float, false, false, true>(h, a) : launch_fused<float, false, false, false>(h, a);
-    }
+    int rc = (h->form == DL_FORM_FP16) ? dispatch<__half, true>(h, a, les, fmode)
+                                       : dispatch<float, false>(h, a, les, fmode);
     if (rc != DL_OK) return rc;
+    if (fmode == F_SPECTRAL) h->fsp.par = 1 - h->fsp.par;
     h->cur = n;
     h->step = step;
     return DL_OK;

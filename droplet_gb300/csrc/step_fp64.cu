@@ -342,7 +342,7 @@ __global__ void __launch_bounds__(256) collide_fp64(const Fp64Args a) {
     // NaN is skipped by the reference's comparisons; exclude it here as well
     const double vmin = (active && ph == ph) ? ph : INFINITY;
     const double vmax = (active && ph == ph) ? ph : -INFINITY;
-    minmax_block_and_finalize<double>(a.st, vmin, vmax, a.maco, 0.0, N, a.phi1, a.phi2, bad, a.step);
+    minmax_block_and_finalize<double>(a.st, vmin, vmax, a.maco, 0.0, N, a.phi1, a.phi2, bad, a.step, gridDim.x);
 }
 
 // ---------------------------------------------------------------------------

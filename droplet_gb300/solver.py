@@ -202,6 +202,15 @@ class Droplet(_HandleAPI):
         """Bracket every launch with CUDA events (and reset the counters)."""
         self._call("profile", 1 if enable else 0)
 
+    def set_option(self, key: str, value: int):
+        """Launch-shape knob of the fused kernel (e.g. "lz")."""
+        self._call("set_option", key.encode(), C.c_int64(int(value)))
+
+    def get_option(self, key: str) -> int:
+        v = C.c_int64()
+        self._call("get_option", key.encode(), C.byref(v))
+        return int(v.value)
+
     def profile_read(self) -> dict:
         s = _abi.DLProfileStats()
         self._call("profile_read", C.byref(s))

@@ -193,6 +193,13 @@ int dl_profile(dl_handle* h, int enable);
 /* Synchronise, then report and reset the launch counters and event times. */
 int dl_profile_read(dl_handle* h, dl_profile_stats* out);
 
+/* Launch-shape knobs of the fused kernel (no reference counterpart: the
+ * reference fixes its loop structure at compile time). key "lz": z planes
+ * marched by one block (1..nz); "lz" = 0 restores the default. Read back with
+ * dl_get_option. Returns DL_ERR_ARG for an unknown key or value. */
+int dl_set_option(dl_handle* h, const char* key, int64_t value);
+int dl_get_option(dl_handle* h, const char* key, int64_t* value);
+
 /* Copy the last error message of the handle into buf (NUL-terminated). */
 int dl_last_error(dl_handle* h, char* buf, int buflen);
 

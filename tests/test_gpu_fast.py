@@ -37,6 +37,10 @@ def make_case(case, shape, seed=11):
     elif case == "spectral_les":
         P = P.replace(les=True, Cs=0.1, delta=1.0, eps=1e-6, kc=3)
         mode = _abi.DL_FORCE_SPECTRAL
+    elif case == "spectral_kc4":
+        # more band modes than the in-kernel synthesis holds: separate launches
+        P = P.replace(eps=1e-6, kc=4)
+        mode = _abi.DL_FORCE_SPECTRAL
     elif case == "eta":
         P = P.replace(nu2=0.05)
     return P, f, mode, force
@@ -61,7 +65,7 @@ def errors(P, a, b):
 
 
 @pytest.mark.parametrize("form,tol_phi,tol_u", [(FORM_FP32, 2e-5, 2e-6), (FORM_FP16, 1e-3, 1e-4)])
-@pytest.mark.parametrize("case", ["plain", "walls", "les_static_force", "spectral_les", "eta"])
+@pytest.mark.parametrize("case", ["plain", "walls", "les_static_force", "spectral_les", "spectral_kc4", "eta"])
 def test_fast_form_tracks_oracle(form, tol_phi, tol_u, case):
     """30 steps on a ragged 40 x 20 x 16 grid (x not a multiple of the 32-wide
     tile); tolerances: FP32 2e-5 in phi~, 2e-6 in u; FP16 storage 1e-3, 1e-4."""
