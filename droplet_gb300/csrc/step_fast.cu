@@ -14,10 +14,13 @@
 // fg_cal and physics, with feq/geq, gradients and fnext materialised):
 //   * the block owns a 32 x 8 column tile and marches up a range of z planes;
 //   * phi (and u for the Smagorinsky strain) are staged plane by plane in
-//     shared memory with a two-cell halo (3-plane ring);
+//     shared memory with a two-cell halo, by asynchronous copies issued one
+//     iteration ahead (4-plane ring);
 //   * for every site of the tile plus a one-cell halo a "record" is built
 //     once: dphi, u, the feq bracket dA, S = 3dp - 1.5u^2, 1/tau_g (with the
-//     eddy viscosity), grad(phi), |grad phi|^2 and the body force (3-plane ring);
+//     eddy viscosity), grad(phi) and the body force (4-plane ring); the
+//     records of plane z+2 are built in the same barrier interval as the pull
+//     of plane z, one barrier per plane;
 //   * each thread pulls its 15 f and 15 g from x - c_i (prefetched into
 //     registers before the record stage), collides each at its source from
 //     that source's record (feq_i, geq_i built on the fly, never stored),
@@ -48,7 +51,14 @@ namespace dl {
 constexpr int TX = 32, TY = 8, NT = TX * TY, NWARP = NT / 32;
 constexpr int EX1 = TX + 2, EY1 = TY + 2, P1 = EX1 * EY1;  // record plane (1-cell halo)
 constexpr int EX2 = TX + 4, EY2 = TY + 4, P2 = EX2 * EY2;  // staging plane (2-cell halo)
-enum { R_DPHI, R_U1, R_U2, R_U3, R_DA, R_S, R_OMG, R_GX, R_GY, R_GZ, R_GSQ, R_DP0, R_FX, R_FY, R_FZ, NR };
+enum { R_DPHI, R_U1, R_U2, R_U3, R_DA, R_S, R_OMG, R_GX, R_GY, R_GZ, R_NBASE };
+// record layout: the base fields, then dp0 (FP16 residual form), then the force
+template <bool RES, bool FORCE>
+struct RecLayout {
+    static constexpr int DP0 = R_NBASE;
+    static constexpr int FX = R_NBASE + (RES ? 1 : 0);
+    static constexpr int NR = FX + (FORCE ? 3 : 0);
+};
 enum { F_NONE = 0, F_ARRAY = 1, F_SPECTRAL = 2 };
 constexpr int SK = 2;                 // in-kernel spectral forcing: |k_x| <= 2 (kc <= 3)
 constexpr int SNK = 2 * SK + 1;
@@ -278,20 +288,41 @@ __device__ void spectral_finalize(const FastArgs& a) {
 }
 
 // ---- the fused step kernel ---------------------------------------------------
+// Per z plane one barrier: staging ring and record ring have four slots; the
+// records of plane z+2 are built in the same phase as the pull of plane z.
+constexpr int NSLOT = 4;
+
+__device__ __forceinline__ void cp_async4(float* smem_dst, const float* gmem_src) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem_src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// shared-memory footprint (floats) of the fused kernel
+__host__ __device__ constexpr int fused_smem_floats(bool les, bool spec, int nr) {
+    return NSLOT * P2 + (les ? NSLOT * 3 * P2 : 0) + NSLOT * nr * P1 +
+           (spec ? 2 * (2 * 3 * SNK * EY1) + 2 * (SNK * EX1 + SNK * EY1) : 0);
+}
+
 template <typename ST, bool RES, bool LES, int FMODE>
-__global__ void __launch_bounds__(NT, 2) step_fused(const FastArgs a) {
+__device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int bx, int by, int bz, unsigned nblk) {
     constexpr bool FORCE = FMODE != F_NONE;
     constexpr bool SPEC = FMODE == F_SPECTRAL;
-    extern __shared__ float smem[];
-    float* s_phi = smem;                            // [3][P2]
-    float* s_u = s_phi + 3 * P2;                    // [3][3][P2] (LES)
-    float* s_rec = s_u + (LES ? 9 * P2 : 0);        // [3][NR][P1]
-    float2* s_C = (float2*)(s_rec + 3 * NR * P1);   // [3][SNK][EY1] (SPEC)
+    using RL = RecLayout<RES, FORCE>;
+    constexpr int NR = RL::NR;
+    float* s_phi = smem;                                  // [NSLOT][P2]
+    float* s_u = s_phi + NSLOT * P2;                      // [NSLOT][3][P2] (LES)
+    float* s_rec = s_u + (LES ? NSLOT * 3 * P2 : 0);      // [NSLOT][NR][P1]
+    float2* s_C = (float2*)(s_rec + NSLOT * NR * P1);     // [2][3][SNK][EY1] (SPEC)
+    float2* s_tx = s_C + 2 * 3 * SNK * EY1;               // [SNK][EX1] e^{i kx x}
+    float2* s_ty = s_tx + SNK * EX1;                      // [SNK][EY1] e^{i ky y}
     const int tid = threadIdx.x;
     const int tx = tid % TX, ty = tid / TX, lane = tid & 31;
     const int nx = a.nx, ny = a.ny, nz = a.nz;
-    const long long N = a.N;
-    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * a.lz;
+    const unsigned N = (unsigned)a.N;
+    const unsigned nxy = (unsigned)nx * (unsigned)ny;
+    const int x0 = bx * TX, y0 = by * TY, z0 = bz * a.lz;
     const int z1 = min(z0 + a.lz, nz);
     float mn, mx;
     if (a.visc_fixed) {
@@ -301,58 +332,103 @@ __global__ void __launch_bounds__(NT, 2) step_fused(const FastArgs a) {
         mn = (float)a.st->phi_min;
         mx = (float)a.st->phi_max;
     }
+    // ---- per-thread wrapped offsets (computed once) ----
+    // staging positions k = tid, tid + NT (P2 = 432 < 2 NT)
+    unsigned soff[2];
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+        const int k = tid + j * NT;
+        const int ex = k % EX2, ey = k / EX2;
+        soff[j] = k < P2 ? (unsigned)pmod(x0 - 2 + ex, nx) + (unsigned)nx * (unsigned)pmod(y0 - 2 + ey, ny) : 0u;
+    }
+    // record positions k = tid, tid + NT (P1 = 340 < 2 NT)
+    unsigned roff[2];
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+        const int k = tid + j * NT;
+        const int ex = k % EX1, ey = k / EX1;
+        roff[j] = k < P1 ? (unsigned)pmod(x0 - 1 + ex, nx) + (unsigned)nx * (unsigned)pmod(y0 - 1 + ey, ny) : 0u;
+    }
+    // destination column and its wrapped neighbours
+    const int gxd = x0 + tx, gyd = y0 + ty;
+    const bool act = gxd < nx && gyd < ny;
+    unsigned xs[3], yr[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        xs[d] = (unsigned)pmod(gxd - 1 + d, nx);
+        yr[d] = (unsigned)nx * (unsigned)pmod(gyd - 1 + d, ny);
+    }
+    // twiddle tables of the in-kernel forcing for this block's columns and rows
+    if (SPEC) {
+        for (int t = tid; t < SNK * EX1; t += NT) {
+            const int kxi = t / EX1, ex = t % EX1;
+            s_tx[t] = a.twx[pmod((kxi - SK) * pmod(x0 - 1 + ex, nx), nx)];
+        }
+        for (int t = tid; t < SNK * EY1; t += NT) {
+            const int kyi = t / EY1, ey = t % EY1;
+            s_ty[t] = a.twy[pmod((kyi - SK) * pmod(y0 - 1 + ey, ny), ny)];
+        }
+    }
 
-    auto stage = [&](int zz) {
-        const int slot = (zz + 3) % 3;
-        const int zw = pmod(zz, nz);
-        for (int k = tid; k < P2; k += NT) {
-            const int ex = k % EX2, ey = k / EX2;
-            const long long s = pmod(x0 - 2 + ex, nx) + (long long)nx * (pmod(y0 - 2 + ey, ny) + (long long)ny * zw);
-            s_phi[slot * P2 + k] = __ldg(a.mac + s);
+    auto stage = [&](int zz) {  // asynchronous copy of plane zz (wrapped) into its slot
+        const int slot = (zz + NSLOT) % NSLOT;
+        const unsigned zo = (unsigned)pmod(zz, nz) * nxy;
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            const int k = tid + j * NT;
+            if (k >= P2) continue;
+            const unsigned s = zo + soff[j];
+            cp_async4(s_phi + slot * P2 + k, a.mac + s);
             if (LES) {
-                s_u[(slot * 3 + 0) * P2 + k] = __ldg(a.mac + N + s);
-                s_u[(slot * 3 + 1) * P2 + k] = __ldg(a.mac + 2 * N + s);
-                s_u[(slot * 3 + 2) * P2 + k] = __ldg(a.mac + 3 * N + s);
+                cp_async4(s_u + (slot * 3 + 0) * P2 + k, a.mac + N + s);
+                cp_async4(s_u + (slot * 3 + 1) * P2 + k, a.mac + 2 * N + s);
+                cp_async4(s_u + (slot * 3 + 2) * P2 + k, a.mac + 3 * N + s);
             }
         }
+        cp_async_commit();
     };
 
-    // force synthesis table of plane zr: C[c][kx][row] = sum over the modes
-    // with this kx of w f_hat e^{i (ky y + kz z)}
+    // force synthesis table of plane zr: C[c][kx][row] = sum over the modes with
+    // this kx of w f_hat e^{i (ky y + kz z)}
     auto ctable = [&](int zr) {
+        float2* C = s_C + ((zr + 2) & 1) * (3 * SNK * EY1);
         const int zw = pmod(zr, nz);
         for (int t = tid; t < 3 * SNK * EY1; t += NT) {
             const int yy = t % EY1, r = t / EY1, kxi = r % SNK, c = r / SNK;
-            const int yg = pmod(y0 - 1 + yy, ny);
             float re = 0.f, im = 0.f;
             for (int m = a.kx_off[kxi]; m < a.kx_off[kxi + 1]; ++m) {
                 const int4 md = a.modes[m];
-                const float2 ey = a.twy[pmod(md.y * yg, ny)];
-                const float2 ez = a.twz[pmod(md.z * zw, nz)];
+                const float2 ey = s_ty[(md.y + SK) * EY1 + yy];
+                int iz = md.z * zw;
+                iz = iz >= nz ? iz - nz : iz;
+                const float2 ez = a.twz[iz];
                 const float pr = ey.x * ez.x - ey.y * ez.y, pi = ey.x * ez.y + ey.y * ez.x;
                 const float2 fv = a.fh[c * a.nm + m];
                 re += fv.x * pr - fv.y * pi;
                 im += fv.x * pi + fv.y * pr;
             }
-            s_C[t] = make_float2(re, im);
+            C[t] = make_float2(re, im);
         }
     };
 
     auto records = [&](int zr) {
-        const int sc = (zr + 3) % 3, sm1 = (zr + 2) % 3, sp1 = (zr + 4) % 3;
-        float* R = s_rec + ((zr + 3) % 3) * NR * P1;
-        const int zw = pmod(zr, nz);
-        for (int k = tid; k < P1; k += NT) {
-            const int ex = k % EX1, ey = k / EX1;
-            const int c2 = (ey + 1) * EX2 + (ex + 1);
+        const int sc = (zr + NSLOT) % NSLOT, sm1 = (zr + NSLOT - 1) % NSLOT, sp1 = (zr + 1) % NSLOT;
+        float* R = s_rec + sc * NR * P1;
+        const float2* C = s_C + ((zr + 2) & 1) * (3 * SNK * EY1);
+        const unsigned zo = (unsigned)pmod(zr, nz) * nxy;
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            const int k = tid + j * NT;
+            if (k >= P1) continue;
+            const int rex = k % EX1, rey = k / EX1;
+            const int c2 = (rey + 1) * EX2 + (rex + 1);
             float v[Q];
 #pragma unroll
             for (int i = 1; i < Q; ++i) {
                 const int sl = cz(i) == 0 ? sc : (cz(i) > 0 ? sp1 : sm1);
                 v[i] = s_phi[sl * P2 + c2 + cy(i) * EX2 + cx(i)];
             }
-            const int xg = pmod(x0 - 1 + ex, nx);
-            const long long s = xg + (long long)nx * (pmod(y0 - 1 + ey, ny) + (long long)ny * zw);
+            const unsigned s = zo + roff[j];
             float u1, u2, u3;
             float w[3][Q];
             if (LES) {
@@ -383,49 +459,52 @@ __global__ void __launch_bounds__(NT, 2) step_fused(const FastArgs a) {
             R[R_GX * P1 + k] = r.gx;
             R[R_GY * P1 + k] = r.gy;
             R[R_GZ * P1 + k] = r.gz;
-            R[R_GSQ * P1 + k] = r.gsq;
-            if (RES) R[R_DP0 * P1 + k] = r.dp0;
+            if (RES) R[RL::DP0 * P1 + k] = r.dp0;
             if (FMODE == F_ARRAY) {
-                R[R_FX * P1 + k] = __ldg(a.force + s);
-                R[R_FY * P1 + k] = __ldg(a.force + N + s);
-                R[R_FZ * P1 + k] = __ldg(a.force + 2 * N + s);
+                R[RL::FX * P1 + k] = __ldg(a.force + s);
+                R[(RL::FX + 1) * P1 + k] = __ldg(a.force + N + s);
+                R[(RL::FX + 2) * P1 + k] = __ldg(a.force + 2 * N + s);
             } else if (SPEC) {
                 float F[3] = {0.f, 0.f, 0.f};
 #pragma unroll
                 for (int kxi = 0; kxi < SNK; ++kxi) {
-                    const float2 ex_ = a.twx[pmod((kxi - SK) * xg, nx)];
+                    const float2 e = s_tx[kxi * EX1 + rex];
 #pragma unroll
                     for (int c = 0; c < 3; ++c) {
-                        const float2 cv = s_C[(c * SNK + kxi) * EY1 + ey];
-                        F[c] += cv.x * ex_.x - cv.y * ex_.y;
+                        const float2 cv = C[(c * SNK + kxi) * EY1 + rey];
+                        F[c] += cv.x * e.x - cv.y * e.y;
                     }
                 }
-                R[R_FX * P1 + k] = F[0];
-                R[R_FY * P1 + k] = F[1];
-                R[R_FZ * P1 + k] = F[2];
+                R[RL::FX * P1 + k] = F[0];
+                R[(RL::FX + 1) * P1 + k] = F[1];
+                R[(RL::FX + 2) * P1 + k] = F[2];
             }
         }
     };
 
-    // prologue: records of planes z0-1 and z0
+    // ---- prologue: records of planes z0-1, z0, z0+1 ----
     stage(z0 - 2);
     stage(z0 - 1);
     stage(z0);
-    if (SPEC) ctable(z0 - 1);
+    stage(z0 + 1);
+    if (SPEC) {
+        __syncthreads();  // s_ty, s_tx
+        ctable(z0 - 1);
+        ctable(z0);
+    }
+    cp_async_wait_all();
     __syncthreads();
     records(z0 - 1);
-    __syncthreads();
-    stage(z0 + 1);
-    if (SPEC) ctable(z0);
-    __syncthreads();
     records(z0);
     __syncthreads();
+    stage(z0 + 2);
+    if (SPEC) ctable(z0 + 1);
+    cp_async_wait_all();
+    __syncthreads();
+    records(z0 + 1);
 
-    const int gxd = x0 + tx, gyd = y0 + ty;
-    const bool act = gxd < nx && gyd < ny;
-    double bmin = INFINITY, bmax = -INFINITY;
+    float bmin = INFINITY, bmax = -INFINITY;
     bool bad = false;
-    // band projection of the new u: lane l accumulates modes l and l + 32
     float pacc[2][3][2];
 #pragma unroll
     for (int j = 0; j < 2; ++j)
@@ -433,28 +512,30 @@ __global__ void __launch_bounds__(NT, 2) step_fused(const FastArgs a) {
         for (int c = 0; c < 3; ++c) pacc[j][c][0] = pacc[j][c][1] = 0.f;
 
     for (int z = z0; z < z1; ++z) {
+        stage(z + 3);
         // populations of the destination plane, pulled from x - c_i
+        unsigned zo[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) zo[d] = (unsigned)pmod(z - 1 + d, nz) * nxy;
         float fin[Q], gin[Q];
         if (act) {
 #pragma unroll
             for (int i = 0; i < Q; ++i) {
-                const long long src = wrapi(gxd - cx(i), nx) +
-                                      (long long)nx * (wrapi(gyd - cy(i), ny) + (long long)ny * wrapi(z - cz(i), nz));
-                fin[i] = Pop<ST>::ld(a.f, i * N + src);
-                gin[i] = Pop<ST>::ld(a.g, i * N + src);
+                const unsigned src = zo[1 - cz(i)] + yr[1 - cy(i)] + xs[1 - cx(i)];
+                fin[i] = Pop<ST>::ld(a.f, (unsigned)i * N + src);
+                gin[i] = Pop<ST>::ld(a.g, (unsigned)i * N + src);
             }
         }
-        stage(z + 2);
-        if (SPEC) ctable(z + 1);
+        if (SPEC) ctable(z + 2);
+        cp_async_wait_all();
         __syncthreads();
-        records(z + 1);
-        __syncthreads();
+        records(z + 2);
         float u1n = 0.f, u2n = 0.f, u3n = 0.f;
         if (act) {
             float fo[Q], go[Q];
 #pragma unroll
             for (int i = 0; i < Q; ++i) {
-                const float* R = s_rec + ((z - cz(i) + 3) % 3) * NR * P1;
+                const float* R = s_rec + ((z - cz(i) + NSLOT) % NSLOT) * NR * P1;
                 const int k = (ty + 1 - cy(i)) * EX1 + (tx + 1 - cx(i));
                 Rec r;
                 r.dphi = R[R_DPHI * P1 + k];
@@ -467,12 +548,12 @@ __global__ void __launch_bounds__(NT, 2) step_fused(const FastArgs a) {
                 r.gx = R[R_GX * P1 + k];
                 r.gy = R[R_GY * P1 + k];
                 r.gz = R[R_GZ * P1 + k];
-                r.gsq = R[R_GSQ * P1 + k];
-                r.dp0 = RES ? R[R_DP0 * P1 + k] : 0.f;
+                r.gsq = r.gx * r.gx + r.gy * r.gy + r.gz * r.gz;
+                r.dp0 = RES ? R[RL::DP0 * P1 + k] : 0.f;
                 if (FORCE) {
-                    r.Fx = R[R_FX * P1 + k];
-                    r.Fy = R[R_FY * P1 + k];
-                    r.Fz = R[R_FZ * P1 + k];
+                    r.Fx = R[RL::FX * P1 + k];
+                    r.Fy = R[(RL::FX + 1) * P1 + k];
+                    r.Fz = R[(RL::FX + 2) * P1 + k];
                 } else {
                     r.Fx = r.Fy = r.Fz = 0.f;
                 }
@@ -509,7 +590,7 @@ __global__ void __launch_bounds__(NT, 2) step_fused(const FastArgs a) {
                 else if (cz(i) == -1) u3n -= go[i];
             }
             dpn *= (1.0f / 3.0f);
-            const long long d = gxd + (long long)nx * (gyd + (long long)ny * z);
+            const unsigned d = zo[1] + yr[1] + xs[1];
             if (RES) {
                 const float phin = __fadd_rn(a.phi1, dphin);
                 const float dp0n = site_dp0(a, dphin);
@@ -517,14 +598,14 @@ __global__ void __launch_bounds__(NT, 2) step_fused(const FastArgs a) {
 #pragma unroll
                 for (int i = 0; i < Q; ++i) {
                     const float cu = (i == 0) ? 0.f : cdot3(i, u1n, u2n, u3n);
-                    Pop<ST>::st(a.fo, i * N + d, fo[i] - fbar(i, dphin, phin, dp0n, cu));
-                    Pop<ST>::st(a.go, i * N + d, go[i] - gbar(i, Sn, cu));
+                    Pop<ST>::st(a.fo, (unsigned)i * N + d, fo[i] - fbar(i, dphin, phin, dp0n, cu));
+                    Pop<ST>::st(a.go, (unsigned)i * N + d, go[i] - gbar(i, Sn, cu));
                 }
             } else {
 #pragma unroll
                 for (int i = 0; i < Q; ++i) {
-                    Pop<ST>::st(a.fo, i * N + d, fo[i]);
-                    Pop<ST>::st(a.go, i * N + d, go[i]);
+                    Pop<ST>::st(a.fo, (unsigned)i * N + d, fo[i]);
+                    Pop<ST>::st(a.go, (unsigned)i * N + d, go[i]);
                 }
             }
             a.maco[d] = dphin;
@@ -533,19 +614,17 @@ __global__ void __launch_bounds__(NT, 2) step_fused(const FastArgs a) {
             a.maco[3 * N + d] = u3n;
             a.maco[4 * N + d] = dpn;
             const float phin_f = a.phi1 + dphin;
-            if (phin_f == phin_f) {
-                bmin = fmin(bmin, (double)phin_f);
-                bmax = fmax(bmax, (double)phin_f);
-            }
+            bmin = fminf(bmin, phin_f);  // fminf ignores NaN
+            bmax = fmaxf(bmax, phin_f);
             bad |= !(isfinite(dphin) && isfinite(dpn) && isfinite(u1n) && isfinite(u2n) && isfinite(u3n));
         }
         if (SPEC) {
             // x stage of the band projection over this warp's row (one y, one z)
             float sr[3][SK + 1], si[3][SK + 1];
+            const float u[3] = {u1n, u2n, u3n};  // zero for inactive lanes
 #pragma unroll
             for (int k = 0; k <= SK; ++k) {
-                const float2 e = a.twx[pmod(k * gxd, nx)];
-                const float u[3] = {u1n, u2n, u3n};  // zero for inactive lanes
+                const float2 e = s_tx[(k + SK) * EX1 + tx + 1];  // e^{i k x}
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
                     sr[c][k] = u[c] * e.x;
@@ -558,25 +637,31 @@ __global__ void __launch_bounds__(NT, 2) step_fused(const FastArgs a) {
                 for (int c = 0; c < 3; ++c)
 #pragma unroll
                     for (int o = 16; o > 0; o >>= 1) {
-                        sr[c][k] += __shfl_xor_sync(0xffffffffu, sr[c][k], o);
-                        si[c][k] += __shfl_xor_sync(0xffffffffu, si[c][k], o);
+                        if (k == 0) {
+                            sr[c][k] += __shfl_xor_sync(0xffffffffu, sr[c][k], o);
+                        } else {
+                            sr[c][k] += __shfl_xor_sync(0xffffffffu, sr[c][k], o);
+                            si[c][k] += __shfl_xor_sync(0xffffffffu, si[c][k], o);
+                        }
                     }
-            const int yw = pmod(gyd, ny);
 #pragma unroll
             for (int j = 0; j < 2; ++j) {
                 const int m = lane + 32 * j;
                 if (m < a.nm) {
                     const int4 md = a.modes[m];
-                    const float2 ey = a.twy[pmod(md.y * yw, ny)];
-                    const float2 ez = a.twz[pmod(md.z * z, nz)];
-                    // e^{-i (ky y + kz z)}
-                    const float pr = ey.x * ez.x - ey.y * ez.y, pi = -(ey.x * ez.y + ey.y * ez.x);
+                    int iz = md.z * z;
+                    iz = iz >= nz ? iz - nz : iz;
+                    const float2 ez = a.twz[iz];
+                    const float2 ey = s_ty[(md.y + SK) * EY1 + ty + 1];
+                    // e^{-i (ky y + kz z)} = conj(e^{i ky y} e^{i kz z})
+                    const float pr = ey.x * ez.x - ey.y * ez.y;
+                    const float pi = -(ey.x * ez.y + ey.y * ez.x);
                     const int ak = md.x < 0 ? -md.x : md.x;
 #pragma unroll
                     for (int c = 0; c < 3; ++c) {
-                        float xr = 0.f, xi = 0.f;
+                        float xr = sr[c][0], xi = 0.f;
 #pragma unroll
-                        for (int k = 0; k <= SK; ++k)
+                        for (int k = 1; k <= SK; ++k)
                             if (k == ak) {
                                 xr = sr[c][k];
                                 xi = si[c][k];
@@ -613,10 +698,16 @@ __global__ void __launch_bounds__(NT, 2) step_fused(const FastArgs a) {
         }
         __threadfence();  // the last block reads acc after every block's ticket
     }
-    const unsigned nblk = gridDim.x * gridDim.y * gridDim.z;
-    const bool last = minmax_block_and_finalize<float>(a.st, bmin, bmax, a.maco, a.phi1, N, (double)a.phi1,
-                                                       (double)a.phi2, bad, a.step, nblk);
+    const bool last = minmax_block_and_finalize<float>(a.st, (double)bmin, (double)bmax, a.maco, a.phi1, a.N,
+                                                       (double)a.phi1, (double)a.phi2, bad, a.step, nblk);
     if (SPEC && last) spectral_finalize(a);
+}
+
+template <typename ST, bool RES, bool LES, int FMODE>
+__global__ void __launch_bounds__(NT, 2) step_fused(const FastArgs a) {
+    extern __shared__ float smem[];
+    fused_body<ST, RES, LES, FMODE>(a, smem, blockIdx.x, blockIdx.y, blockIdx.z,
+                                    gridDim.x * gridDim.y * gridDim.z);
 }
 
 // ---- initial populations f = feq, g = geq at every site (ini :244-251) -------
@@ -789,10 +880,9 @@ __global__ void sp_fhat_from_uh(const double* __restrict__ uh, int K, const int4
 }
 
 // ---- host side ---------------------------------------------------------------------
-static size_t smem_bytes(bool les, int fmode) {
-    size_t n = 3 * P2 + (les ? 9 * P2 : 0) + 3 * NR * P1;
-    if (fmode == F_SPECTRAL) n += 2 * 3 * SNK * EY1;
-    return sizeof(float) * n;
+template <bool RES, bool LES, int FMODE>
+static size_t smem_bytes() {
+    return sizeof(float) * (size_t)fused_smem_floats(LES, FMODE == F_SPECTRAL, RecLayout<RES, FMODE != F_NONE>::NR);
 }
 
 static void fill_fast(dl_handle* h, FastArgs& a) {
@@ -1006,7 +1096,7 @@ template <typename ST, bool RES, bool LES, int FMODE>
 static int launch_fused(dl_handle* h, const FastArgs& a) {
     static bool configured[64] = {false};
     const int dev = h->device & 63;
-    const size_t sm = smem_bytes(LES, FMODE);
+    const size_t sm = smem_bytes<RES, LES, FMODE>();
     if (!configured[dev]) {
         DL_CUDA(h, cudaFuncSetAttribute(step_fused<ST, RES, LES, FMODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)sm));
