@@ -345,6 +345,89 @@ def run_ours(args):
     return 0
 
 
+def run_ensemble(args):
+    """config4: 64 members of uneven size stepped by one persistent launch per
+    step (CUDA-graph replay), against the same members one launch at a time."""
+    import torch
+    from droplet_gb300 import autotune, configs
+    from droplet_gb300.ensemble import Ensemble
+    from droplet_gb300.solver import Droplet
+
+    torch.cuda.set_device(0)
+    form = FORMS[args.form]
+    ws = configs.ensemble_members(n_members=args.members, form=form)
+    sites = sum(w.n_sites for w in ws)
+    stream = torch.cuda.Stream()
+    ens = Ensemble([w.params for w in ws], [w.shape for w in ws], form)
+    ens.set_stream(stream.cuda_stream)
+    for mem, w in zip(ens.members, ws):
+        mem.set_fields(**w.fields)
+        mem.init_equilibrium()
+        mem.set_force(w.force_mode)
+    tune = autotune.tune_ensemble(ens)
+    ens.step(args.warmup + (args.warmup % 2))
+    ens.sync()
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    time.sleep(0.3)
+    ens.profile(True)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    ens.step(args.steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    prof = ens.profile_read()
+    ens.profile(False)
+    clk = clocks.stop()
+    ens.sync()
+    value = sites * args.steps / (ms / 1e3) / 1e6
+    ens.close()
+    # the same members, one launch per member per step
+    k_seq = min(args.steps, 40)
+    solos = []
+    for w in ws:
+        d = Droplet(w.params, w.shape, form)
+        d.set_stream(stream.cuda_stream)
+        d.set_fields(**w.fields)
+        d.init_equilibrium()
+        d.set_force(w.force_mode)
+        d.set_option("lz", tune["lz"])
+        d.step(2)
+        solos.append(d)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(k_seq):
+        for d in solos:
+            d.step(1)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_seq = e0.elapsed_time(e1)
+    seq = sites * k_seq / (ms_seq / 1e3) / 1e6
+    for d in solos:
+        d.close()
+    peak, peak_kind = measured_peak_gbs()
+    achieved = BYTES_PER_SITE[form] * sites / (ms / args.steps / 1e3) / 1e9
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 5), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": DTYPE[form], "data": "synthetic (seeded)",
+        "config": {"workload": f"ensemble_{len(ws)}_members", "form": args.form, "sites": sites,
+                   "member_sizes": sorted({w.shape[0] for w in ws}), "seed": 4,
+                   "sequential_mlups": round(seq, 3), "batched_over_sequential": round(value / seq, 3),
+                   "tune": {k: v for k, v in tune.items() if k != "timings"},
+                   "l2": "inputs larger than L2"},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": None, "peak_source": peak_kind,
+                     "kernel": "step_batched", "kernel_ms": round(ms / args.steps, 5)},
+        "cpu_baseline": None, "e2e": None, "clocks": clk, "gpu_launches": int(prof["launches"]),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -356,11 +439,14 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--members", type=int, default=64)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "config4":
+        return run_ensemble(args)
     return run_ours(args)
 
 

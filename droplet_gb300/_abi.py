@@ -154,6 +154,20 @@ def declare(lib: C.CDLL, prefix: str) -> None:
         lib.dl_set_option.restype = C.c_int
         lib.dl_get_option.argtypes = [h, C.c_char_p, C.POINTER(C.c_int64)]
         lib.dl_get_option.restype = C.c_int
+        lib.dl_batch_create.argtypes = [C.POINTER(DLParams), C.POINTER(C.c_int), C.c_int, C.c_int, C.POINTER(_vp)]
+        lib.dl_batch_create.restype = C.c_int
+        lib.dl_batch_member.argtypes = [_vp, C.c_int, C.POINTER(_vp)]
+        lib.dl_batch_member.restype = C.c_int
+        lib.dl_batch_set_stream.argtypes = [_vp, _vp]
+        lib.dl_batch_set_stream.restype = C.c_int
+        lib.dl_batch_step.argtypes = [_vp, C.c_int]
+        lib.dl_batch_step.restype = C.c_int
+        lib.dl_batch_set_option.argtypes = [_vp, C.c_char_p, C.c_int64]
+        lib.dl_batch_set_option.restype = C.c_int
+        lib.dl_batch_get_option.argtypes = [_vp, C.c_char_p, C.POINTER(C.c_int64)]
+        lib.dl_batch_get_option.restype = C.c_int
+        lib.dl_batch_destroy.argtypes = [_vp]
+        lib.dl_batch_destroy.restype = C.c_int
     else:
         lib.orc_get_force.argtypes = [h, _dp, _dp, _dp]
         lib.orc_get_force.restype = C.c_int
@@ -189,4 +203,11 @@ HEADER_SYMBOLS = [
     "dl_profile_read",
     "dl_set_option",
     "dl_get_option",
+    "dl_batch_create",
+    "dl_batch_member",
+    "dl_batch_set_stream",
+    "dl_batch_step",
+    "dl_batch_set_option",
+    "dl_batch_get_option",
+    "dl_batch_destroy",
 ]

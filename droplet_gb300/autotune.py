@@ -1,0 +1,122 @@
+"""Autotuner for the launch shape of the fused step.
+
+The tunable knobs are those of the C-ABI: for one domain the number of z
+planes a block marches ("lz", ``dl_set_option``); for an ensemble also the
+number of persistent blocks per SM ("blocks_per_sm", ``dl_batch_set_option``).
+Each candidate is timed with the library's own per-launch CUDA events after a
+few warm-up steps; the fastest is applied and cached in a JSON file keyed by
+the GPU, the form and the member shapes, so later runs reuse it without
+timing. The cache lives at $DROPLET_GB300_TUNE_CACHE or
+~/.cache/droplet_gb300/tune.json.
+"""
+from __future__ import annotations
+
+import json
+import os
+import threading
+
+LZ_CANDIDATES = (4, 8, 16, 32)
+BPS_CANDIDATES = (1, 2)
+_lock = threading.Lock()
+
+
+def cache_path() -> str:
+    p = os.environ.get("DROPLET_GB300_TUNE_CACHE")
+    if p:
+        return p
+    return os.path.join(os.path.expanduser("~"), ".cache", "droplet_gb300", "tune.json")
+
+
+def _load() -> dict:
+    try:
+        with open(cache_path()) as fh:
+            return json.load(fh)
+    except Exception:
+        return {}
+
+
+def _store(key: str, value: dict) -> None:
+    with _lock:
+        d = _load()
+        d[key] = value
+        p = cache_path()
+        os.makedirs(os.path.dirname(p), exist_ok=True)
+        tmp = p + ".tmp"
+        with open(tmp, "w") as fh:
+            json.dump(d, fh, indent=1, sort_keys=True)
+        os.replace(tmp, p)
+
+
+def gpu_name() -> str:
+    try:
+        import torch
+
+        return torch.cuda.get_device_name(torch.cuda.current_device())
+    except Exception:
+        return "unknown-gpu"
+
+
+def _time_steps(obj, steps: int) -> float:
+    obj.step(3)
+    obj.profile(True)
+    obj.step(steps)
+    s = obj.profile_read()
+    obj.profile(False)
+    return s["main_ms"] / steps
+
+
+def _key(kind: str, form: int, shapes, extra: str) -> str:
+    sig = ",".join("x".join(str(v) for v in s) for s in sorted(tuple(s) for s in shapes))
+    return f"{kind}|{gpu_name()}|form{form}|{extra}|{sig}"
+
+
+def tune_droplet(sim, steps: int = 20, use_cache: bool = True) -> dict:
+    """Pick "lz" for one Droplet (fast forms). Returns the chosen settings."""
+    p = sim.params
+    key = _key("single", sim.form, [(sim.nx, sim.ny, sim.nz)], f"les{int(bool(p.les))}")
+    if use_cache:
+        hit = _load().get(key)
+        if hit:
+            sim.set_option("lz", hit["lz"])
+            return dict(hit, cached=True)
+    best = None
+    timings = {}
+    for lz in LZ_CANDIDATES:
+        if lz > sim.nz:
+            continue
+        sim.set_option("lz", lz)
+        ms = _time_steps(sim, steps)
+        timings[str(lz)] = ms
+        if best is None or ms < best[1]:
+            best = (lz, ms)
+    sim.set_option("lz", best[0])
+    res = {"lz": best[0], "ms_per_step": best[1], "timings": timings}
+    _store(key, res)
+    return dict(res, cached=False)
+
+
+def tune_ensemble(ens, steps: int = 10, use_cache: bool = True) -> dict:
+    """Pick "lz" and "blocks_per_sm" for an Ensemble."""
+    shapes = [(m.nx, m.ny, m.nz) for m in ens.members]
+    key = _key("batch", ens.form, shapes, f"les{int(bool(ens.members[0].params.les))}")
+    if use_cache:
+        hit = _load().get(key)
+        if hit:
+            ens.set_option("lz", hit["lz"])
+            ens.set_option("blocks_per_sm", hit["blocks_per_sm"])
+            return dict(hit, cached=True)
+    best = None
+    timings = {}
+    for bps in BPS_CANDIDATES:
+        for lz in LZ_CANDIDATES:
+            ens.set_option("lz", lz)
+            ens.set_option("blocks_per_sm", bps)
+            ms = _time_steps(ens, steps)
+            timings[f"lz{lz}_bps{bps}"] = ms
+            if best is None or ms < best[2]:
+                best = (lz, bps, ms)
+    ens.set_option("lz", best[0])
+    ens.set_option("blocks_per_sm", best[1])
+    res = {"lz": best[0], "blocks_per_sm": best[1], "ms_per_step": best[2], "timings": timings}
+    _store(key, res)
+    return dict(res, cached=False)

@@ -128,4 +128,31 @@ def config3(seed: int = 3) -> Workload:
     return w
 
 
-WORKLOADS = {"config1": config1, "config2": config2, "config3": config3}
+def ensemble_members(n_members: int = 64, seed: int = 4, sizes=(48, 64, 96), webers=(2.0, 5.0, 10.0, 20.0),
+                     urms: float = 0.01, form: int = _abi.DL_FORM_FP32):
+    """Members of the batched ensemble: grid L drawn uniformly from ``sizes``,
+    droplet radius 0.15 L at the centre plus a uniform offset within +-4
+    cells, Weber number drawn from ``webers``, its own forcing-phase seed.
+    Physics as the forced-turbulence case (LES, band forcing)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for m in range(n_members):
+        L = int(rng.choice(sizes))
+        We = float(rng.choice(webers))
+        off = rng.uniform(-4.0, 4.0, size=3)
+        c = (L - 1) / 2.0
+        mseed = int(rng.integers(0, 2**31 - 1))
+        w = forced_turbulence(n=L, centers=[tuple(c + off)], radius=0.15 * L, We=We, urms=urms, seed=mseed,
+                              form=form, steps=2000)
+        w.name = f"member{m}_L{L}_We{We:g}"
+        out.append(w)
+    return out
+
+
+def config4(n_members: int = 64, seed: int = 4):
+    """64 FP32 members, L in {48, 64, 96}, R = 0.15 L, We in {2, 5, 10, 20},
+    offsets within +-4 cells, 2000 steps."""
+    return ensemble_members(n_members=n_members, seed=seed)
+
+
+WORKLOADS = {"config1": config1, "config2": config2, "config3": config3, "config4": config4}

@@ -448,3 +448,80 @@ int dl_last_error(dl_handle* h, char* buf, int buflen) {
 }
 
 }  // extern "C"
+
+// ---- batched ensembles ------------------------------------------------------
+struct dl_batch {
+    int nm;
+    dl_handle** mem;
+    void* impl;
+};
+
+extern "C" {
+
+int dl_batch_create(const dl_params* params, const int* dims, int nmembers, int form, dl_batch** out) {
+    if (!params || !dims || !out || nmembers < 1) return DL_ERR_ARG;
+    *out = nullptr;
+    if (form != DL_FORM_FP32 && form != DL_FORM_FP16) return DL_ERR_UNSUPPORTED;
+    for (int m = 1; m < nmembers; ++m)
+        if ((params[m].les != 0) != (params[0].les != 0)) return DL_ERR_ARG;
+    dl_batch* b = new (std::nothrow) dl_batch();
+    if (!b) return DL_ERR_ALLOC;
+    b->nm = nmembers;
+    b->mem = (dl_handle**)calloc((size_t)nmembers, sizeof(dl_handle*));
+    if (!b->mem) {
+        delete b;
+        return DL_ERR_ALLOC;
+    }
+    int rc = DL_OK;
+    for (int m = 0; m < nmembers && rc == DL_OK; ++m)
+        rc = dl_create(&params[m], dims[3 * m], dims[3 * m + 1], dims[3 * m + 2], form, &b->mem[m]);
+    if (rc == DL_OK) rc = batch_create(b->mem, nmembers, &b->impl);
+    if (rc != DL_OK) {
+        dl_batch_destroy(b);
+        return rc;
+    }
+    *out = b;
+    return DL_OK;
+}
+
+int dl_batch_member(dl_batch* b, int m, dl_handle** member) {
+    if (!b || !member || m < 0 || m >= b->nm) return DL_ERR_ARG;
+    *member = b->mem[m];
+    return DL_OK;
+}
+
+int dl_batch_set_stream(dl_batch* b, void* stream) {
+    if (!b) return DL_ERR_ARG;
+    for (int m = 0; m < b->nm; ++m) b->mem[m]->stream = (cudaStream_t)stream;
+    return DL_OK;
+}
+
+int dl_batch_step(dl_batch* b, int nsteps) {
+    if (!b || nsteps < 0) return DL_ERR_ARG;
+    return batch_step(b->impl, nsteps);
+}
+
+int dl_batch_set_option(dl_batch* b, const char* key, int64_t value) {
+    if (!b || !key) return DL_ERR_ARG;
+    return batch_set_option(b->impl, key, (long long)value);
+}
+
+int dl_batch_get_option(dl_batch* b, const char* key, int64_t* value) {
+    if (!b || !key || !value) return DL_ERR_ARG;
+    long long v = 0;
+    int rc = batch_get_option(b->impl, key, &v);
+    if (rc == DL_OK) *value = (int64_t)v;
+    return rc;
+}
+
+int dl_batch_destroy(dl_batch* b) {
+    if (!b) return DL_ERR_ARG;
+    if (b->impl) batch_destroy(b->impl);
+    for (int m = 0; m < b->nm; ++m)
+        if (b->mem[m]) dl_destroy(b->mem[m]);
+    free(b->mem);
+    delete b;
+    return DL_OK;
+}
+
+}  // extern "C"

@@ -50,6 +50,8 @@ struct DevState {
     // spectral forcing
     double sp_energy;                // band energy of the last forcing evaluation
     double sp_coef;                  // 0.5 eps / E
+    unsigned int sp_done;            // last-block ticket of the band projection
+    unsigned int pad2_;
 };
 
 // Ordered mapping of a double to a signed 64-bit key (monotone for non-NaN).
@@ -174,6 +176,12 @@ int fast_set_populations(dl_handle* h, const double* d_f, const double* d_g);
 int fast_step(dl_handle* h);
 int fast_prepare_force(dl_handle* h, int mode);
 int spectral_project_f32(dl_handle* h, const float* d_u1, const float* d_u2, const float* d_u3);
+// batched ensembles of fast-form handles (step_fast.cu)
+int batch_create(dl_handle** members, int nm, void** out);
+void batch_destroy(void* b);
+int batch_step(void* b, int nsteps);
+int batch_set_option(void* b, const char* key, long long v);
+int batch_get_option(void* b, const char* key, long long* v);
 // transposes (layout.cu)
 int soa_to_aos(dl_handle* h, const double* d_soa, double* d_aos);
 int aos_to_soa(dl_handle* h, const double* d_aos, double* d_soa);

@@ -44,6 +44,7 @@
 #include <cuda_fp16.h>
 #include <math.h>
 #include <string.h>
+#include <algorithm>
 #include <vector>
 
 namespace dl {
@@ -52,13 +53,7 @@ constexpr int TX = 32, TY = 8, NT = TX * TY, NWARP = NT / 32;
 constexpr int EX1 = TX + 2, EY1 = TY + 2, P1 = EX1 * EY1;  // record plane (1-cell halo)
 constexpr int EX2 = TX + 4, EY2 = TY + 4, P2 = EX2 * EY2;  // staging plane (2-cell halo)
 enum { R_DPHI, R_U1, R_U2, R_U3, R_DA, R_S, R_OMG, R_GX, R_GY, R_GZ, R_NBASE };
-// record layout: the base fields, then dp0 (FP16 residual form), then the force
-template <bool RES, bool FORCE>
-struct RecLayout {
-    static constexpr int DP0 = R_NBASE;
-    static constexpr int FX = R_NBASE + (RES ? 1 : 0);
-    static constexpr int NR = FX + (FORCE ? 3 : 0);
-};
+
 enum { F_NONE = 0, F_ARRAY = 1, F_SPECTRAL = 2 };
 constexpr int SK = 2;                 // in-kernel spectral forcing: |k_x| <= 2 (kc <= 3)
 constexpr int SNK = 2 * SK + 1;
@@ -288,8 +283,11 @@ __device__ void spectral_finalize(const FastArgs& a) {
 }
 
 // ---- the fused step kernel ---------------------------------------------------
-// Per z plane one barrier: staging ring and record ring have four slots; the
-// records of plane z+2 are built in the same phase as the pull of plane z.
+// Per z plane one barrier: the staging ring and the record ring have four
+// slots; the records of plane z+2 are built in the same barrier interval as
+// the pull of plane z. Records are float4 groups:
+//   q0 = (dphi, u1, u2, u3), q1 = (gx, gy, gz, dA), q2 = (S, 1/tau_g, dp0, Fx),
+//   q3 = (Fy, Fz) (with a force only).
 constexpr int NSLOT = 4;
 
 __device__ __forceinline__ void cp_async4(float* smem_dst, const float* gmem_src) {
@@ -300,25 +298,54 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
 // shared-memory footprint (floats) of the fused kernel
-__host__ __device__ constexpr int fused_smem_floats(bool les, bool spec, int nr) {
-    return NSLOT * P2 + (les ? NSLOT * 3 * P2 : 0) + NSLOT * nr * P1 +
+__host__ __device__ constexpr int fused_smem_floats(bool les, bool spec, bool force) {
+    return NSLOT * P2 * (les ? 4 : 1) + NSLOT * P1 * (12 + (force ? 2 : 0)) +
            (spec ? 2 * (2 * 3 * SNK * EY1) + 2 * (SNK * EX1 + SNK * EY1) : 0);
+}
+
+// the thread's (at most two) record positions: pass A = its own column
+// (rows 0..7, cols 0..31), pass B = rows 8..9 and columns 32..33
+struct RecPos {
+    int k, ex, ey;
+    bool has;
+};
+__device__ __forceinline__ RecPos rec_pos(int tid, int j) {
+    RecPos r;
+    if (j == 0) {
+        r.ex = tid % TX;
+        r.ey = tid / TX;
+        r.has = true;
+    } else if (tid < 2 * TX) {
+        r.ex = tid % TX;
+        r.ey = TY + tid / TX;
+        r.has = true;
+    } else if (tid < 2 * TX + 2 * EY1) {
+        r.ex = TX + (tid - 2 * TX) % 2;
+        r.ey = (tid - 2 * TX) / 2;
+        r.has = true;
+    } else {
+        r.ex = r.ey = 0;
+        r.has = false;
+    }
+    r.k = r.ey * EX1 + r.ex;
+    return r;
 }
 
 template <typename ST, bool RES, bool LES, int FMODE>
 __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int bx, int by, int bz, unsigned nblk) {
     constexpr bool FORCE = FMODE != F_NONE;
     constexpr bool SPEC = FMODE == F_SPECTRAL;
-    using RL = RecLayout<RES, FORCE>;
-    constexpr int NR = RL::NR;
-    float* s_phi = smem;                                  // [NSLOT][P2]
-    float* s_u = s_phi + NSLOT * P2;                      // [NSLOT][3][P2] (LES)
-    float* s_rec = s_u + (LES ? NSLOT * 3 * P2 : 0);      // [NSLOT][NR][P1]
-    float2* s_C = (float2*)(s_rec + NSLOT * NR * P1);     // [2][3][SNK][EY1] (SPEC)
-    float2* s_tx = s_C + 2 * 3 * SNK * EY1;               // [SNK][EX1] e^{i kx x}
-    float2* s_ty = s_tx + SNK * EX1;                      // [SNK][EY1] e^{i ky y}
+    constexpr int NSTG = LES ? 4 : 1;                    // staged fields: phi (+ u1, u2, u3)
+    float* s_stg = smem;                                 // [NSLOT][NSTG][P2]
+    float4* s_q0 = (float4*)(s_stg + NSLOT * NSTG * P2); // [NSLOT][P1]
+    float4* s_q1 = s_q0 + NSLOT * P1;
+    float4* s_q2 = s_q1 + NSLOT * P1;
+    float2* s_q3 = (float2*)(s_q2 + NSLOT * P1);         // [NSLOT][P1] (FORCE)
+    float2* s_C = s_q3 + (FORCE ? NSLOT * P1 : 0);       // [2][3][SNK][EY1] (SPEC)
+    float2* s_tx = s_C + 2 * 3 * SNK * EY1;              // [SNK][EX1] e^{i kx x}
+    float2* s_ty = s_tx + SNK * EX1;                     // [SNK][EY1] e^{i ky y}
     const int tid = threadIdx.x;
-    const int tx = tid % TX, ty = tid / TX, lane = tid & 31;
+    const int tx = tid % TX, ty = tid / TX;
     const int nx = a.nx, ny = a.ny, nz = a.nz;
     const unsigned N = (unsigned)a.N;
     const unsigned nxy = (unsigned)nx * (unsigned)ny;
@@ -333,23 +360,19 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
         mx = (float)a.st->phi_max;
     }
     // ---- per-thread wrapped offsets (computed once) ----
-    // staging positions k = tid, tid + NT (P2 = 432 < 2 NT)
-    unsigned soff[2];
+    unsigned soff[2];  // staging positions k = tid, tid + NT (P2 = 432 < 2 NT)
 #pragma unroll
     for (int j = 0; j < 2; ++j) {
         const int k = tid + j * NT;
         const int ex = k % EX2, ey = k / EX2;
         soff[j] = k < P2 ? (unsigned)pmod(x0 - 2 + ex, nx) + (unsigned)nx * (unsigned)pmod(y0 - 2 + ey, ny) : 0u;
     }
-    // record positions k = tid, tid + NT (P1 = 340 < 2 NT)
-    unsigned roff[2];
+    unsigned roff[2];  // record positions
 #pragma unroll
     for (int j = 0; j < 2; ++j) {
-        const int k = tid + j * NT;
-        const int ex = k % EX1, ey = k / EX1;
-        roff[j] = k < P1 ? (unsigned)pmod(x0 - 1 + ex, nx) + (unsigned)nx * (unsigned)pmod(y0 - 1 + ey, ny) : 0u;
+        const RecPos rp = rec_pos(tid, j);
+        roff[j] = rp.has ? (unsigned)pmod(x0 - 1 + rp.ex, nx) + (unsigned)nx * (unsigned)pmod(y0 - 1 + rp.ey, ny) : 0u;
     }
-    // destination column and its wrapped neighbours
     const int gxd = x0 + tx, gyd = y0 + ty;
     const bool act = gxd < nx && gyd < ny;
     unsigned xs[3], yr[3];
@@ -358,7 +381,6 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
         xs[d] = (unsigned)pmod(gxd - 1 + d, nx);
         yr[d] = (unsigned)nx * (unsigned)pmod(gyd - 1 + d, ny);
     }
-    // twiddle tables of the in-kernel forcing for this block's columns and rows
     if (SPEC) {
         for (int t = tid; t < SNK * EX1; t += NT) {
             const int kxi = t / EX1, ex = t % EX1;
@@ -369,6 +391,23 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
             s_ty[t] = a.twy[pmod((kyi - SK) * pmod(y0 - 1 + ey, ny), ny)];
         }
     }
+    // record-site values read from HBM one plane ahead (p, and u without LES)
+    float pf_dp[2], pf_u[2][3];
+    auto prefetch = [&](int zr) {
+        const unsigned zo = (unsigned)pmod(zr, nz) * nxy;
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            const bool has = j == 0 || tid < 2 * TX + 2 * EY1;
+            if (!has) continue;
+            const unsigned s = zo + roff[j];
+            pf_dp[j] = __ldg(a.mac + 4 * N + s);
+            if (!LES) {
+                pf_u[j][0] = __ldg(a.mac + N + s);
+                pf_u[j][1] = __ldg(a.mac + 2 * N + s);
+                pf_u[j][2] = __ldg(a.mac + 3 * N + s);
+            }
+        }
+    };
 
     auto stage = [&](int zz) {  // asynchronous copy of plane zz (wrapped) into its slot
         const int slot = (zz + NSLOT) % NSLOT;
@@ -378,11 +417,12 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
             const int k = tid + j * NT;
             if (k >= P2) continue;
             const unsigned s = zo + soff[j];
-            cp_async4(s_phi + slot * P2 + k, a.mac + s);
+            float* dst = s_stg + slot * NSTG * P2 + k;
+            cp_async4(dst, a.mac + s);
             if (LES) {
-                cp_async4(s_u + (slot * 3 + 0) * P2 + k, a.mac + N + s);
-                cp_async4(s_u + (slot * 3 + 1) * P2 + k, a.mac + 2 * N + s);
-                cp_async4(s_u + (slot * 3 + 2) * P2 + k, a.mac + 3 * N + s);
+                cp_async4(dst + P2, a.mac + N + s);
+                cp_async4(dst + 2 * P2, a.mac + 2 * N + s);
+                cp_async4(dst + 3 * P2, a.mac + 3 * N + s);
             }
         }
         cp_async_commit();
@@ -393,17 +433,19 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
     auto ctable = [&](int zr) {
         float2* C = s_C + ((zr + 2) & 1) * (3 * SNK * EY1);
         const int zw = pmod(zr, nz);
+        int i1 = zw, i2 = 2 * zw;
+        i2 = i2 >= nz ? i2 - nz : i2;
+        const float2 ez1 = a.twz[i1], ez2 = a.twz[i2];
         for (int t = tid; t < 3 * SNK * EY1; t += NT) {
             const int yy = t % EY1, r = t / EY1, kxi = r % SNK, c = r / SNK;
             float re = 0.f, im = 0.f;
-            for (int m = a.kx_off[kxi]; m < a.kx_off[kxi + 1]; ++m) {
-                const int4 md = a.modes[m];
+            const int m1 = a.kx_off[kxi + 1];
+            for (int m = a.kx_off[kxi]; m < m1; ++m) {
+                const int4 md = __ldg(a.modes + m);
                 const float2 ey = s_ty[(md.y + SK) * EY1 + yy];
-                int iz = md.z * zw;
-                iz = iz >= nz ? iz - nz : iz;
-                const float2 ez = a.twz[iz];
+                const float2 ez = md.z == 0 ? make_float2(1.f, 0.f) : (md.z == 1 ? ez1 : ez2);
                 const float pr = ey.x * ez.x - ey.y * ez.y, pi = ey.x * ez.y + ey.y * ez.x;
-                const float2 fv = a.fh[c * a.nm + m];
+                const float2 fv = __ldg(a.fh + c * a.nm + m);
                 re += fv.x * pr - fv.y * pi;
                 im += fv.x * pi + fv.y * pr;
             }
@@ -413,72 +455,62 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
 
     auto records = [&](int zr) {
         const int sc = (zr + NSLOT) % NSLOT, sm1 = (zr + NSLOT - 1) % NSLOT, sp1 = (zr + 1) % NSLOT;
-        float* R = s_rec + sc * NR * P1;
         const float2* C = s_C + ((zr + 2) & 1) * (3 * SNK * EY1);
-        const unsigned zo = (unsigned)pmod(zr, nz) * nxy;
+        const float* stc = s_stg + sc * NSTG * P2;
+        const float* stm = s_stg + sm1 * NSTG * P2;
+        const float* stp = s_stg + sp1 * NSTG * P2;
 #pragma unroll
         for (int j = 0; j < 2; ++j) {
-            const int k = tid + j * NT;
-            if (k >= P1) continue;
-            const int rex = k % EX1, rey = k / EX1;
-            const int c2 = (rey + 1) * EX2 + (rex + 1);
+            const RecPos rp = rec_pos(tid, j);
+            if (!rp.has) continue;
+            const int c2 = (rp.ey + 1) * EX2 + (rp.ex + 1);
             float v[Q];
 #pragma unroll
             for (int i = 1; i < Q; ++i) {
-                const int sl = cz(i) == 0 ? sc : (cz(i) > 0 ? sp1 : sm1);
-                v[i] = s_phi[sl * P2 + c2 + cy(i) * EX2 + cx(i)];
+                const float* st = cz(i) == 0 ? stc : (cz(i) > 0 ? stp : stm);
+                v[i] = st[c2 + cy(i) * EX2 + cx(i)];
             }
-            const unsigned s = zo + roff[j];
             float u1, u2, u3;
             float w[3][Q];
             if (LES) {
-                u1 = s_u[(sc * 3 + 0) * P2 + c2];
-                u2 = s_u[(sc * 3 + 1) * P2 + c2];
-                u3 = s_u[(sc * 3 + 2) * P2 + c2];
+                u1 = stc[P2 + c2];
+                u2 = stc[2 * P2 + c2];
+                u3 = stc[3 * P2 + c2];
 #pragma unroll
                 for (int c = 0; c < 3; ++c)
 #pragma unroll
                     for (int i = 1; i < Q; ++i) {
-                        const int sl = cz(i) == 0 ? sc : (cz(i) > 0 ? sp1 : sm1);
-                        w[c][i] = s_u[(sl * 3 + c) * P2 + c2 + cy(i) * EX2 + cx(i)];
+                        const float* st = cz(i) == 0 ? stc : (cz(i) > 0 ? stp : stm);
+                        w[c][i] = st[(1 + c) * P2 + c2 + cy(i) * EX2 + cx(i)];
                     }
             } else {
-                u1 = __ldg(a.mac + N + s);
-                u2 = __ldg(a.mac + 2 * N + s);
-                u3 = __ldg(a.mac + 3 * N + s);
+                u1 = pf_u[j][0];
+                u2 = pf_u[j][1];
+                u3 = pf_u[j][2];
             }
-            const float dp = __ldg(a.mac + 4 * N + s);
-            Rec r = make_record<LES>(a, s_phi[sc * P2 + c2], v, w, u1, u2, u3, dp, mn, mx);
-            R[R_DPHI * P1 + k] = r.dphi;
-            R[R_U1 * P1 + k] = r.u1;
-            R[R_U2 * P1 + k] = r.u2;
-            R[R_U3 * P1 + k] = r.u3;
-            R[R_DA * P1 + k] = r.dA;
-            R[R_S * P1 + k] = r.S;
-            R[R_OMG * P1 + k] = r.omg;
-            R[R_GX * P1 + k] = r.gx;
-            R[R_GY * P1 + k] = r.gy;
-            R[R_GZ * P1 + k] = r.gz;
-            if (RES) R[RL::DP0 * P1 + k] = r.dp0;
+            const Rec r = make_record<LES>(a, stc[c2], v, w, u1, u2, u3, pf_dp[j], mn, mx);
+            float F[3] = {0.f, 0.f, 0.f};
             if (FMODE == F_ARRAY) {
-                R[RL::FX * P1 + k] = __ldg(a.force + s);
-                R[(RL::FX + 1) * P1 + k] = __ldg(a.force + N + s);
-                R[(RL::FX + 2) * P1 + k] = __ldg(a.force + 2 * N + s);
+                const unsigned s = (unsigned)pmod(zr, nz) * nxy + roff[j];
+                F[0] = __ldg(a.force + s);
+                F[1] = __ldg(a.force + N + s);
+                F[2] = __ldg(a.force + 2 * N + s);
             } else if (SPEC) {
-                float F[3] = {0.f, 0.f, 0.f};
 #pragma unroll
                 for (int kxi = 0; kxi < SNK; ++kxi) {
-                    const float2 e = s_tx[kxi * EX1 + rex];
+                    const float2 e = s_tx[kxi * EX1 + rp.ex];
 #pragma unroll
                     for (int c = 0; c < 3; ++c) {
-                        const float2 cv = C[(c * SNK + kxi) * EY1 + rey];
+                        const float2 cv = C[(c * SNK + kxi) * EY1 + rp.ey];
                         F[c] += cv.x * e.x - cv.y * e.y;
                     }
                 }
-                R[RL::FX * P1 + k] = F[0];
-                R[(RL::FX + 1) * P1 + k] = F[1];
-                R[(RL::FX + 2) * P1 + k] = F[2];
             }
+            const int o = sc * P1 + rp.k;
+            s_q0[o] = make_float4(r.dphi, r.u1, r.u2, r.u3);
+            s_q1[o] = make_float4(r.gx, r.gy, r.gz, r.dA);
+            s_q2[o] = make_float4(r.S, r.omg, RES ? r.dp0 : 0.f, F[0]);
+            if (FORCE) s_q3[o] = make_float2(F[1], F[2]);
         }
     };
 
@@ -487,6 +519,7 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
     stage(z0 - 1);
     stage(z0);
     stage(z0 + 1);
+    prefetch(z0 - 1);
     if (SPEC) {
         __syncthreads();  // s_ty, s_tx
         ctable(z0 - 1);
@@ -495,21 +528,19 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
     cp_async_wait_all();
     __syncthreads();
     records(z0 - 1);
+    prefetch(z0);
     records(z0);
+    prefetch(z0 + 1);
     __syncthreads();
     stage(z0 + 2);
     if (SPEC) ctable(z0 + 1);
     cp_async_wait_all();
     __syncthreads();
     records(z0 + 1);
+    prefetch(z0 + 2);
 
     float bmin = INFINITY, bmax = -INFINITY;
     bool bad = false;
-    float pacc[2][3][2];
-#pragma unroll
-    for (int j = 0; j < 2; ++j)
-#pragma unroll
-        for (int c = 0; c < 3; ++c) pacc[j][c][0] = pacc[j][c][1] = 0.f;
 
     for (int z = z0; z < z1; ++z) {
         stage(z + 3);
@@ -530,30 +561,31 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
         cp_async_wait_all();
         __syncthreads();
         records(z + 2);
-        float u1n = 0.f, u2n = 0.f, u3n = 0.f;
+        prefetch(z + 3);
         if (act) {
             float fo[Q], go[Q];
 #pragma unroll
             for (int i = 0; i < Q; ++i) {
-                const float* R = s_rec + ((z - cz(i) + NSLOT) % NSLOT) * NR * P1;
-                const int k = (ty + 1 - cy(i)) * EX1 + (tx + 1 - cx(i));
+                const int o = ((z - cz(i) + NSLOT) % NSLOT) * P1 + (ty + 1 - cy(i)) * EX1 + (tx + 1 - cx(i));
+                const float4 q0 = s_q0[o], q1 = s_q1[o], q2 = s_q2[o];
                 Rec r;
-                r.dphi = R[R_DPHI * P1 + k];
-                r.u1 = R[R_U1 * P1 + k];
-                r.u2 = R[R_U2 * P1 + k];
-                r.u3 = R[R_U3 * P1 + k];
-                r.dA = R[R_DA * P1 + k];
-                r.S = R[R_S * P1 + k];
-                r.omg = R[R_OMG * P1 + k];
-                r.gx = R[R_GX * P1 + k];
-                r.gy = R[R_GY * P1 + k];
-                r.gz = R[R_GZ * P1 + k];
+                r.dphi = q0.x;
+                r.u1 = q0.y;
+                r.u2 = q0.z;
+                r.u3 = q0.w;
+                r.gx = q1.x;
+                r.gy = q1.y;
+                r.gz = q1.z;
+                r.dA = q1.w;
+                r.S = q2.x;
+                r.omg = q2.y;
+                r.dp0 = q2.z;
                 r.gsq = r.gx * r.gx + r.gy * r.gy + r.gz * r.gz;
-                r.dp0 = RES ? R[RL::DP0 * P1 + k] : 0.f;
                 if (FORCE) {
-                    r.Fx = R[RL::FX * P1 + k];
-                    r.Fy = R[(RL::FX + 1) * P1 + k];
-                    r.Fz = R[(RL::FX + 2) * P1 + k];
+                    const float2 q3 = s_q3[o];
+                    r.Fx = q2.w;
+                    r.Fy = q3.x;
+                    r.Fz = q3.y;
                 } else {
                     r.Fx = r.Fy = r.Fz = 0.f;
                 }
@@ -577,7 +609,7 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
                 }
             }
             // moments (physics, program/lbm_drop_xy.f90:541-552)
-            float dphin = 0.f, dpn = 0.f;
+            float dphin = 0.f, dpn = 0.f, u1n = 0.f, u2n = 0.f, u3n = 0.f;
 #pragma unroll
             for (int i = 0; i < Q; ++i) {
                 dphin += fo[i];
@@ -618,89 +650,9 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
             bmax = fmaxf(bmax, phin_f);
             bad |= !(isfinite(dphin) && isfinite(dpn) && isfinite(u1n) && isfinite(u2n) && isfinite(u3n));
         }
-        if (SPEC) {
-            // x stage of the band projection over this warp's row (one y, one z)
-            float sr[3][SK + 1], si[3][SK + 1];
-            const float u[3] = {u1n, u2n, u3n};  // zero for inactive lanes
-#pragma unroll
-            for (int k = 0; k <= SK; ++k) {
-                const float2 e = s_tx[(k + SK) * EX1 + tx + 1];  // e^{i k x}
-#pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    sr[c][k] = u[c] * e.x;
-                    si[c][k] = -u[c] * e.y;
-                }
-            }
-#pragma unroll
-            for (int k = 0; k <= SK; ++k)
-#pragma unroll
-                for (int c = 0; c < 3; ++c)
-#pragma unroll
-                    for (int o = 16; o > 0; o >>= 1) {
-                        if (k == 0) {
-                            sr[c][k] += __shfl_xor_sync(0xffffffffu, sr[c][k], o);
-                        } else {
-                            sr[c][k] += __shfl_xor_sync(0xffffffffu, sr[c][k], o);
-                            si[c][k] += __shfl_xor_sync(0xffffffffu, si[c][k], o);
-                        }
-                    }
-#pragma unroll
-            for (int j = 0; j < 2; ++j) {
-                const int m = lane + 32 * j;
-                if (m < a.nm) {
-                    const int4 md = a.modes[m];
-                    int iz = md.z * z;
-                    iz = iz >= nz ? iz - nz : iz;
-                    const float2 ez = a.twz[iz];
-                    const float2 ey = s_ty[(md.y + SK) * EY1 + ty + 1];
-                    // e^{-i (ky y + kz z)} = conj(e^{i ky y} e^{i kz z})
-                    const float pr = ey.x * ez.x - ey.y * ez.y;
-                    const float pi = -(ey.x * ez.y + ey.y * ez.x);
-                    const int ak = md.x < 0 ? -md.x : md.x;
-#pragma unroll
-                    for (int c = 0; c < 3; ++c) {
-                        float xr = sr[c][0], xi = 0.f;
-#pragma unroll
-                        for (int k = 1; k <= SK; ++k)
-                            if (k == ak) {
-                                xr = sr[c][k];
-                                xi = si[c][k];
-                            }
-                        if (md.x < 0) xi = -xi;
-                        pacc[j][c][0] += xr * pr - xi * pi;
-                        pacc[j][c][1] += xr * pi + xi * pr;
-                    }
-                }
-            }
-        }
     }
-    if (SPEC) {
-        // block sum of the warps' projections, then one FP64 atomic per value
-        __syncthreads();
-        float* red = s_rec;  // [NWARP][3][SMAXM][2], the record ring is free now
-        const int warp = tid >> 5;
-#pragma unroll
-        for (int j = 0; j < 2; ++j) {
-            const int m = lane + 32 * j;
-            if (m < a.nm)
-#pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    red[((warp * 3 + c) * SMAXM + m) * 2 + 0] = pacc[j][c][0];
-                    red[((warp * 3 + c) * SMAXM + m) * 2 + 1] = pacc[j][c][1];
-                }
-        }
-        __syncthreads();
-        for (int t = tid; t < 3 * a.nm * 2; t += NT) {
-            const int part = t & 1, cm = t >> 1, c = cm / a.nm, m = cm % a.nm;
-            float s = 0.f;
-            for (int w = 0; w < NWARP; ++w) s += red[((w * 3 + c) * SMAXM + m) * 2 + part];
-            atomicAdd(a.acc + 2 * (c * a.nm + m) + part, (double)s);
-        }
-        __threadfence();  // the last block reads acc after every block's ticket
-    }
-    const bool last = minmax_block_and_finalize<float>(a.st, (double)bmin, (double)bmax, a.maco, a.phi1, a.N,
-                                                       (double)a.phi1, (double)a.phi2, bad, a.step, nblk);
-    if (SPEC && last) spectral_finalize(a);
+    minmax_block_and_finalize<float>(a.st, (double)bmin, (double)bmax, a.maco, a.phi1, a.N, (double)a.phi1,
+                                     (double)a.phi2, bad, a.step, nblk);
 }
 
 template <typename ST, bool RES, bool LES, int FMODE>
@@ -708,6 +660,125 @@ __global__ void __launch_bounds__(NT, 2) step_fused(const FastArgs a) {
     extern __shared__ float smem[];
     fused_body<ST, RES, LES, FMODE>(a, smem, blockIdx.x, blockIdx.y, blockIdx.z,
                                     gridDim.x * gridDim.y * gridDim.z);
+}
+
+// ---- band projection of the new u (F_SPECTRAL) ---------------------------------------
+// acc[c][m] += sum over sites of u_c e^{-i k_m.x}: one warp per (y, z) row,
+// lanes over x with the x twiddles, warp sums, then each lane owns two band
+// modes and applies e^{-i (ky y + kz z)}; block sum and one FP64 atomic per
+// value; the block that finishes last turns acc into the next coefficients.
+constexpr int PROJ_NT = 256;
+
+__device__ void project_rows(const FastArgs& a, long long row0, long long row1, unsigned nblk) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nx = a.nx, ny = a.ny, nz = a.nz;
+    const long long N = a.N;
+    const float* u[3] = {a.maco + N, a.maco + 2 * N, a.maco + 3 * N};
+    float pacc[2][3][2];
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) pacc[j][c][0] = pacc[j][c][1] = 0.f;
+    for (long long row = row0 + warp; row < row1; row += PROJ_NT / 32) {
+        const int z = (int)(row / ny), y = (int)(row - (long long)z * ny);
+        const long long base = row * nx;
+        float sr[3][SK + 1], si[3][SK + 1];
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+#pragma unroll
+            for (int k = 0; k <= SK; ++k) sr[c][k] = si[c][k] = 0.f;
+        for (int x = lane; x < nx; x += 32) {
+            float uv[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) uv[c] = u[c][base + x];
+#pragma unroll
+            for (int k = 1; k <= SK; ++k) {
+                int ix = k * x;
+                ix = ix >= nx ? ix - nx : ix;
+                const float2 e = a.twx[ix];
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    sr[c][k] += uv[c] * e.x;
+                    si[c][k] -= uv[c] * e.y;
+                }
+            }
+#pragma unroll
+            for (int c = 0; c < 3; ++c) sr[c][0] += uv[c];
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+#pragma unroll
+            for (int k = 0; k <= SK; ++k)
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    sr[c][k] += __shfl_xor_sync(0xffffffffu, sr[c][k], o);
+                    if (k > 0) si[c][k] += __shfl_xor_sync(0xffffffffu, si[c][k], o);
+                }
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            const int m = lane + 32 * j;
+            if (m >= a.nm) continue;
+            const int4 md = __ldg(a.modes + m);
+            int iy = md.y * y;
+            iy = iy < 0 ? iy + ny : iy;
+            iy = iy >= ny ? iy - ny : iy;
+            int iz = md.z * z;
+            iz = iz >= nz ? iz - nz : iz;
+            const float2 ey = a.twy[iy], ez = a.twz[iz];
+            const float pr = ey.x * ez.x - ey.y * ez.y;
+            const float pi = -(ey.x * ez.y + ey.y * ez.x);
+            const int ak = md.x < 0 ? -md.x : md.x;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                float xr = sr[c][0], xi = 0.f;
+#pragma unroll
+                for (int k = 1; k <= SK; ++k)
+                    if (k == ak) {
+                        xr = sr[c][k];
+                        xi = si[c][k];
+                    }
+                if (md.x < 0) xi = -xi;
+                pacc[j][c][0] += xr * pr - xi * pi;
+                pacc[j][c][1] += xr * pi + xi * pr;
+            }
+        }
+    }
+    __shared__ float red[PROJ_NT / 32][3][SMAXM][2];
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+        const int m = lane + 32 * j;
+        if (m < a.nm)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                red[warp][c][m][0] = pacc[j][c][0];
+                red[warp][c][m][1] = pacc[j][c][1];
+            }
+    }
+    __syncthreads();
+    for (int t = tid; t < 3 * a.nm * 2; t += PROJ_NT) {
+        const int part = t & 1, cm = t >> 1, c = cm / a.nm, m = cm % a.nm;
+        float s = 0.f;
+        for (int w = 0; w < PROJ_NT / 32; ++w) s += red[w][c][m][part];
+        atomicAdd(a.acc + 2 * (c * a.nm + m) + part, (double)s);
+    }
+    __threadfence();
+    __shared__ int s_last;
+    __syncthreads();
+    if (tid == 0) {
+        const unsigned t = atomicAdd(&a.st->sp_done, 1u);
+        s_last = (t == nblk - 1);
+    }
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    spectral_finalize(a);
+    if (tid == 0) a.st->sp_done = 0u;
+}
+
+__global__ void __launch_bounds__(PROJ_NT) sp_project_fast(const FastArgs a, int rows_per_block) {
+    const long long rows = (long long)a.ny * a.nz;
+    const long long r0 = (long long)blockIdx.x * rows_per_block;
+    project_rows(a, r0, min(r0 + rows_per_block, rows), gridDim.x);
 }
 
 // ---- initial populations f = feq, g = geq at every site (ini :244-251) -------
@@ -882,7 +953,7 @@ __global__ void sp_fhat_from_uh(const double* __restrict__ uh, int K, const int4
 // ---- host side ---------------------------------------------------------------------
 template <bool RES, bool LES, int FMODE>
 static size_t smem_bytes() {
-    return sizeof(float) * (size_t)fused_smem_floats(LES, FMODE == F_SPECTRAL, RecLayout<RES, FMODE != F_NONE>::NR);
+    return sizeof(float) * (size_t)fused_smem_floats(LES, FMODE == F_SPECTRAL, FMODE != F_NONE);
 }
 
 static void fill_fast(dl_handle* h, FastArgs& a) {
@@ -1092,6 +1163,16 @@ static int fast_spectral_project(dl_handle* h) {
     return DL_OK;
 }
 
+static const int PROJ_ROWS = 64;  // rows of the band projection per block
+
+static int launch_projection(dl_handle* h, const FastArgs& a) {
+    const long long rows = (long long)a.ny * a.nz;
+    const unsigned grid = (unsigned)((rows + PROJ_ROWS - 1) / PROJ_ROWS);
+    DL_LAUNCH(h, false, (sp_project_fast<<<grid, PROJ_NT, 0, h->stream>>>(a, PROJ_ROWS)));
+    DL_CUDA(h, cudaGetLastError());
+    return DL_OK;
+}
+
 template <typename ST, bool RES, bool LES, int FMODE>
 static int launch_fused(dl_handle* h, const FastArgs& a) {
     static bool configured[64] = {false};
@@ -1105,6 +1186,7 @@ static int launch_fused(dl_handle* h, const FastArgs& a) {
     dim3 grid((a.nx + TX - 1) / TX, (a.ny + TY - 1) / TY, (a.nz + a.lz - 1) / a.lz);
     DL_LAUNCH(h, true, (step_fused<ST, RES, LES, FMODE><<<grid, NT, sm, h->stream>>>(a)));
     DL_CUDA(h, cudaGetLastError());
+    if (FMODE == F_SPECTRAL) return launch_projection(h, a);
     return DL_OK;
 }
 
@@ -1120,29 +1202,20 @@ static int dispatch(dl_handle* h, const FastArgs& a, bool les, int fmode) {
     return launch_fused<ST, RES, false, F_NONE>(h, a);
 }
 
-int fast_step(dl_handle* h) {
-    const int c = h->cur, n = 1 - c;
-    const long long step = h->step + 1;
-    int fmode = F_NONE;
-    if (h->force_mode == DL_FORCE_STATIC) {
-        fmode = F_ARRAY;
-    } else if (h->force_mode == DL_FORCE_SPECTRAL) {
-        if (h->fsp.nm > 0) {
-            fmode = F_SPECTRAL;
-            if (h->fsp.dirty) {
-                int rc = fast_spectral_project(h);
-                if (rc != DL_OK) return rc;
-            }
-        } else {
-            fmode = F_ARRAY;
-            const float* m = h->mac32[c];
-            int rc = spectral_force_f32(h, m + h->N, m + 2 * h->N, m + 3 * h->N, h->force32, h->force32 + h->N,
-                                        h->force32 + 2 * h->N);
-            if (rc != DL_OK) return rc;
-        }
-    }
-    FastArgs a;
+// Step arguments of handle h for the state k steps ahead (k = 0 or 1):
+// buffers, band coefficients and wall terms of that step.
+static int force_fmode(const dl_handle* h) {
+    if (h->force_mode == DL_FORCE_STATIC) return F_ARRAY;
+    if (h->force_mode == DL_FORCE_SPECTRAL) return h->fsp.nm > 0 ? F_SPECTRAL : F_ARRAY;
+    return F_NONE;
+}
+
+static void make_step_args(dl_handle* h, int k, FastArgs& a) {
+    const int c = h->cur ^ k, n = 1 - c;
+    const long long step = h->step + 1 + k;
     fill_fast(h, a);
+    a.fh = h->fsp.d_fh[h->fsp.par ^ k];
+    a.fh_next = h->fsp.d_fh[1 - (h->fsp.par ^ k)];
     a.mac = h->mac32[c];
     a.maco = h->mac32[n];
     a.f = h->fs[c];
@@ -1152,21 +1225,342 @@ int fast_step(dl_handle* h) {
     a.step = step;
     double U[3] = {0.0, 0.0, 0.0};
     if (step >= h->P.wall_start)
-        for (int k = 0; k < 3; ++k) U[k] = h->P.wall_u[k];
+        for (int q = 0; q < 3; ++q) U[q] = h->P.wall_u[q];
     const int bot_src[5] = {6, 11, 12, 13, 10}, top_src[5] = {3, 14, 7, 8, 9};
-    for (int k = 0; k < 5; ++k) {
-        int j = bot_src[k];
-        a.wall_bot[k] = (float)(6.0 * h->lc.E[j] * ((-U[0]) * cx(j) + (-U[1]) * cy(j) + (-U[2]) * cz(j)));
-        j = top_src[k];
-        a.wall_top[k] = (float)(6.0 * h->lc.E[j] * (U[0] * cx(j) + U[1] * cy(j) + U[2] * cz(j)));
+    for (int q = 0; q < 5; ++q) {
+        int j = bot_src[q];
+        a.wall_bot[q] = (float)(6.0 * h->lc.E[j] * ((-U[0]) * cx(j) + (-U[1]) * cy(j) + (-U[2]) * cz(j)));
+        j = top_src[q];
+        a.wall_top[q] = (float)(6.0 * h->lc.E[j] * (U[0] * cx(j) + U[1] * cy(j) + U[2] * cz(j)));
     }
-    const bool les = h->P.les != 0;
-    int rc = (h->form == DL_FORM_FP16) ? dispatch<__half, true>(h, a, les, fmode)
-                                       : dispatch<float, false>(h, a, les, fmode);
+}
+
+// work that must precede a fused step: band coefficients of new fields, or
+// the force arrays of the separate-launch spectral path
+static int pre_step(dl_handle* h) {
+    if (h->force_mode != DL_FORCE_SPECTRAL) return DL_OK;
+    if (h->fsp.nm > 0) return h->fsp.dirty ? fast_spectral_project(h) : DL_OK;
+    const float* m = h->mac32[h->cur];
+    return spectral_force_f32(h, m + h->N, m + 2 * h->N, m + 3 * h->N, h->force32, h->force32 + h->N,
+                              h->force32 + 2 * h->N);
+}
+
+static void advance(dl_handle* h, int n) {
+    if (n & 1) {
+        h->cur = 1 - h->cur;
+        if (force_fmode(h) == F_SPECTRAL) h->fsp.par = 1 - h->fsp.par;
+    }
+    h->step += n;
+}
+
+int fast_step(dl_handle* h) {
+    int rc = pre_step(h);
     if (rc != DL_OK) return rc;
-    if (fmode == F_SPECTRAL) h->fsp.par = 1 - h->fsp.par;
-    h->cur = n;
-    h->step = step;
+    FastArgs a;
+    make_step_args(h, 0, a);
+    const int fmode = force_fmode(h);
+    const bool les = h->P.les != 0;
+    rc = (h->form == DL_FORM_FP16) ? dispatch<__half, true>(h, a, les, fmode) : dispatch<float, false>(h, a, les, fmode);
+    if (rc != DL_OK) return rc;
+    advance(h, 1);
+    return DL_OK;
+}
+
+// ---- batched ensembles ----------------------------------------------------------
+// Every member's tiles are work items of ONE persistent launch per step; each
+// block copies its member's arguments into shared memory and runs the same
+// fused body; each member keeps its own reduction state, so its last block
+// finalises it. Optionally two steps are captured in a CUDA graph and replayed.
+template <typename ST, bool RES, bool LES, int FMODE>
+__global__ void __launch_bounds__(NT, 2) step_batched(const FastArgs* __restrict__ table,
+                                                      const int4* __restrict__ items, int nitems,
+                                                      const unsigned* __restrict__ nblk_of) {
+    extern __shared__ float smem[];
+    __shared__ __align__(16) FastArgs s_a;
+    for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
+        __syncthreads();
+        const int4 it = items[w];
+        const int* src = (const int*)(table + it.x);
+        int* dst = (int*)&s_a;
+        for (int t = threadIdx.x; t < (int)(sizeof(FastArgs) / sizeof(int)); t += blockDim.x) dst[t] = src[t];
+        __syncthreads();
+        fused_body<ST, RES, LES, FMODE>(s_a, smem, it.y, it.z, it.w, nblk_of[it.x]);
+    }
+}
+
+// band projection of every member's new u: work items (member, first row)
+__global__ void __launch_bounds__(PROJ_NT) sp_project_batched(const FastArgs* __restrict__ table,
+                                                              const int2* __restrict__ items, int nitems,
+                                                              const unsigned* __restrict__ nblk_of, int rows_per_item) {
+    __shared__ __align__(16) FastArgs s_a;
+    for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
+        __syncthreads();
+        const int2 it = items[w];
+        const int* src = (const int*)(table + it.x);
+        int* dst = (int*)&s_a;
+        for (int t = threadIdx.x; t < (int)(sizeof(FastArgs) / sizeof(int)); t += blockDim.x) dst[t] = src[t];
+        __syncthreads();
+        const long long rows = (long long)s_a.ny * s_a.nz;
+        const long long r0 = (long long)it.y * rows_per_item;
+        project_rows(s_a, r0, min(r0 + rows_per_item, rows), nblk_of[it.x]);
+    }
+}
+
+struct BatchImpl {
+    int nm;
+    int form;
+    dl_handle** mem;
+    FastArgs* h_table;      // [2][nm] host copy
+    FastArgs* d_table;      // [2][nm]
+    int4* d_items;
+    unsigned* d_nblk;
+    int nitems;
+    int2* d_pitems;         // projection work items (member, row block)
+    unsigned* d_pnblk;      // projection blocks per member
+    int npitems;
+    int lz, bps, use_graph;
+    int sms;
+    cudaStream_t stream;
+    cudaGraphExec_t gexec;
+    int graph_ok;
+    int built_parity;       // member parity the tables were built at (-1: rebuild)
+    int fmode, les;
+};
+
+template <typename ST, bool RES, bool LES, int FMODE>
+static int launch_batched_t(dl_handle* h0, BatchImpl* b, int k) {
+    static bool configured[64] = {false};
+    const int dev = h0->device & 63;
+    const size_t sm = smem_bytes<RES, LES, FMODE>();
+    if (!configured[dev]) {
+        DL_CUDA(h0, cudaFuncSetAttribute(step_batched<ST, RES, LES, FMODE>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        configured[dev] = true;
+    }
+    const int grid = min(b->nitems, b->bps * b->sms);
+    step_batched<ST, RES, LES, FMODE><<<grid, NT, sm, b->stream>>>(b->d_table + (size_t)k * b->nm, b->d_items,
+                                                                  b->nitems, b->d_nblk);
+    DL_CUDA(h0, cudaGetLastError());
+    if (FMODE == F_SPECTRAL) {
+        const int pg = min(b->npitems, 4 * b->sms);
+        sp_project_batched<<<pg, PROJ_NT, 0, b->stream>>>(b->d_table + (size_t)k * b->nm, b->d_pitems, b->npitems,
+                                                          b->d_pnblk, PROJ_ROWS);
+        DL_CUDA(h0, cudaGetLastError());
+    }
+    return DL_OK;
+}
+
+template <typename ST, bool RES>
+static int launch_batched_st(dl_handle* h0, BatchImpl* b, int k) {
+    if (b->les) {
+        if (b->fmode == F_SPECTRAL) return launch_batched_t<ST, RES, true, F_SPECTRAL>(h0, b, k);
+        if (b->fmode == F_ARRAY) return launch_batched_t<ST, RES, true, F_ARRAY>(h0, b, k);
+        return launch_batched_t<ST, RES, true, F_NONE>(h0, b, k);
+    }
+    if (b->fmode == F_SPECTRAL) return launch_batched_t<ST, RES, false, F_SPECTRAL>(h0, b, k);
+    if (b->fmode == F_ARRAY) return launch_batched_t<ST, RES, false, F_ARRAY>(h0, b, k);
+    return launch_batched_t<ST, RES, false, F_NONE>(h0, b, k);
+}
+
+static int launch_batched(BatchImpl* b, int k) {
+    dl_handle* h0 = b->mem[0];
+    return b->form == DL_FORM_FP16 ? launch_batched_st<__half, true>(h0, b, k) : launch_batched_st<float, false>(h0, b, k);
+}
+
+int batch_create(dl_handle** members, int nm, void** out) {
+    dl_handle* h0 = members[0];
+    BatchImpl* b = (BatchImpl*)calloc(1, sizeof(BatchImpl));
+    if (!b) return DL_ERR_ALLOC;
+    b->nm = nm;
+    b->form = h0->form;
+    b->mem = members;
+    b->lz = 8;
+    b->bps = 2;
+    b->use_graph = 1;
+    b->stream = h0->stream;
+    b->built_parity = -1;
+    b->les = h0->P.les != 0;
+    cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, h0->device);
+    b->h_table = (FastArgs*)calloc(2 * (size_t)nm, sizeof(FastArgs));
+    if (!b->h_table) {
+        free(b);
+        return DL_ERR_ALLOC;
+    }
+    if (cudaMalloc(&b->d_table, 2 * (size_t)nm * sizeof(FastArgs)) != cudaSuccess ||
+        cudaMalloc(&b->d_nblk, (size_t)nm * sizeof(unsigned)) != cudaSuccess ||
+        cudaMalloc(&b->d_pnblk, (size_t)nm * sizeof(unsigned)) != cudaSuccess) {
+        batch_destroy(b);
+        return DL_ERR_ALLOC;
+    }
+    *out = b;
+    return DL_OK;
+}
+
+void batch_destroy(void* p) {
+    BatchImpl* b = (BatchImpl*)p;
+    if (!b) return;
+    if (b->graph_ok) cudaGraphExecDestroy(b->gexec);
+    cudaFree(b->d_table);
+    cudaFree(b->d_items);
+    cudaFree(b->d_nblk);
+    cudaFree(b->d_pitems);
+    cudaFree(b->d_pnblk);
+    free(b->h_table);
+    free(b);
+}
+
+int batch_set_option(void* p, const char* key, long long v) {
+    BatchImpl* b = (BatchImpl*)p;
+    if (strcmp(key, "lz") == 0) {
+        if (v < 1 || v > 4096) return DL_ERR_ARG;
+        b->lz = (int)v;
+    } else if (strcmp(key, "blocks_per_sm") == 0) {
+        if (v < 1 || v > 2) return DL_ERR_ARG;
+        b->bps = (int)v;
+    } else if (strcmp(key, "graph") == 0) {
+        b->use_graph = v ? 1 : 0;
+    } else {
+        return DL_ERR_ARG;
+    }
+    b->built_parity = -1;  // rebuild tables, items and graph
+    return DL_OK;
+}
+
+int batch_get_option(void* p, const char* key, long long* v) {
+    BatchImpl* b = (BatchImpl*)p;
+    if (strcmp(key, "lz") == 0) *v = b->lz;
+    else if (strcmp(key, "blocks_per_sm") == 0) *v = b->bps;
+    else if (strcmp(key, "graph") == 0) *v = b->use_graph;
+    else return DL_ERR_ARG;
+    return DL_OK;
+}
+
+// (re)build the two argument tables (this step and the next), the work items
+// and the graph for the members' current state
+static int batch_build(BatchImpl* b) {
+    dl_handle* h0 = b->mem[0];
+    const int nm = b->nm;
+    b->fmode = force_fmode(h0);
+    std::vector<int4> items;
+    std::vector<unsigned> nblk(nm);
+    // largest members first: their items are the longest
+    std::vector<int> order(nm);
+    for (int m = 0; m < nm; ++m) order[m] = m;
+    for (int i = 1; i < nm; ++i)
+        for (int j = i; j > 0 && b->mem[order[j]]->N > b->mem[order[j - 1]]->N; --j) std::swap(order[j], order[j - 1]);
+    for (int m = 0; m < nm; ++m) {
+        dl_handle* h = b->mem[m];
+        h->lz = min(b->lz, h->nz);
+        for (int k = 0; k < 2; ++k) make_step_args(h, k, b->h_table[(size_t)k * nm + m]);
+        const int gx = (h->nx + TX - 1) / TX, gy = (h->ny + TY - 1) / TY, gz = (h->nz + h->lz - 1) / h->lz;
+        nblk[m] = (unsigned)(gx * gy * gz);
+    }
+    for (int oi = 0; oi < nm; ++oi) {
+        const int m = order[oi];
+        dl_handle* h = b->mem[m];
+        const int gx = (h->nx + TX - 1) / TX, gy = (h->ny + TY - 1) / TY, gz = (h->nz + h->lz - 1) / h->lz;
+        for (int bz = 0; bz < gz; ++bz)
+            for (int by = 0; by < gy; ++by)
+                for (int bx = 0; bx < gx; ++bx) items.push_back(make_int4(m, bx, by, bz));
+    }
+    if ((int)items.size() != b->nitems || !b->d_items) {
+        cudaFree(b->d_items);
+        b->d_items = nullptr;
+        DL_CUDA(h0, cudaMalloc(&b->d_items, items.size() * sizeof(int4)));
+    }
+    b->nitems = (int)items.size();
+    DL_CUDA(h0, cudaMemcpyAsync(b->d_items, items.data(), items.size() * sizeof(int4), cudaMemcpyHostToDevice, b->stream));
+    // projection items: every member's rows in blocks of PROJ_ROWS
+    std::vector<int2> pitems;
+    std::vector<unsigned> pnblk(nm);
+    for (int m = 0; m < nm; ++m) {
+        const long long rows = (long long)b->mem[m]->ny * b->mem[m]->nz;
+        const int nb = (int)((rows + PROJ_ROWS - 1) / PROJ_ROWS);
+        pnblk[m] = (unsigned)nb;
+        for (int r = 0; r < nb; ++r) pitems.push_back(make_int2(m, r));
+    }
+    if ((int)pitems.size() != b->npitems || !b->d_pitems) {
+        cudaFree(b->d_pitems);
+        b->d_pitems = nullptr;
+        DL_CUDA(h0, cudaMalloc(&b->d_pitems, pitems.size() * sizeof(int2)));
+    }
+    b->npitems = (int)pitems.size();
+    DL_CUDA(h0, cudaMemcpyAsync(b->d_pitems, pitems.data(), pitems.size() * sizeof(int2), cudaMemcpyHostToDevice,
+                                b->stream));
+    DL_CUDA(h0, cudaMemcpyAsync(b->d_pnblk, pnblk.data(), nm * sizeof(unsigned), cudaMemcpyHostToDevice, b->stream));
+    DL_CUDA(h0, cudaMemcpyAsync(b->d_nblk, nblk.data(), nm * sizeof(unsigned), cudaMemcpyHostToDevice, b->stream));
+    DL_CUDA(h0, cudaMemcpyAsync(b->d_table, b->h_table, 2 * (size_t)nm * sizeof(FastArgs), cudaMemcpyHostToDevice,
+                                b->stream));
+    DL_CUDA(h0, cudaStreamSynchronize(b->stream));
+    if (b->graph_ok) {
+        cudaGraphExecDestroy(b->gexec);
+        b->graph_ok = 0;
+    }
+    if (b->use_graph) {
+        cudaGraph_t g;
+        DL_CUDA(h0, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+        int rc = launch_batched(b, 0);
+        if (rc == DL_OK) rc = launch_batched(b, 1);
+        cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+        if (rc != DL_OK) return rc;
+        DL_CUDA(h0, e);
+        e = cudaGraphInstantiate(&b->gexec, g, 0);
+        cudaGraphDestroy(g);
+        DL_CUDA(h0, e);
+        b->graph_ok = 1;
+    }
+    b->built_parity = h0->cur;
+    return DL_OK;
+}
+
+int batch_step(void* p, int nsteps) {
+    BatchImpl* b = (BatchImpl*)p;
+    dl_handle* h0 = b->mem[0];
+    const int nm = b->nm;
+    // members step together: same parity and step count, same kernel variant
+    for (int m = 0; m < nm; ++m) {
+        dl_handle* h = b->mem[m];
+        if (!h->eq_init) return set_error(h0, DL_ERR_STATE, "member %d not initialised", m);
+        if (h->cur != h0->cur || h->step != h0->step || force_fmode(h) != force_fmode(h0) ||
+            (h->fsp.par != h0->fsp.par && force_fmode(h) == F_SPECTRAL) || (h->P.les != 0) != (b->les != 0))
+            return set_error(h0, DL_ERR_STATE, "member %d is not in step with member 0", m);
+        if (h->P.walls && h->P.wall_start > h->step + 1 && h->P.wall_start <= h->step + nsteps)
+            return set_error(h0, DL_ERR_UNSUPPORTED, "wall start inside a batched call; split the call");
+    }
+    for (int m = 0; m < nm; ++m) {
+        const int dirty = b->mem[m]->fsp.dirty;
+        int rc = pre_step(b->mem[m]);
+        if (rc != DL_OK) return rc;
+        if (dirty) b->built_parity = -1;
+    }
+    if (b->built_parity < 0 || b->fmode != force_fmode(h0) || b->stream != h0->stream) {
+        b->stream = h0->stream;
+        int rc = batch_build(b);
+        if (rc != DL_OK) return rc;
+    }
+    // table 0 is the step from the parity the tables were built at, table 1
+    // the step after it; the graph runs table 0 then table 1. (The tables'
+    // absolute step numbers only feed the NaN report and the wall terms,
+    // which are constant inside one call.)
+    int left = nsteps;
+    while (left > 0) {
+        const int k = (h0->cur == b->built_parity) ? 0 : 1;
+        if (b->graph_ok && k == 0 && left >= 2) {
+            launch_begin(h0);
+            DL_CUDA(h0, cudaGraphLaunch(b->gexec, b->stream));
+            launch_end(h0, true);
+            h0->launches += 1;  // the graph holds two step launches
+            for (int m = 0; m < nm; ++m) advance(b->mem[m], 2);
+            left -= 2;
+        } else {
+            launch_begin(h0);
+            int rc = launch_batched(b, k);
+            launch_end(h0, true);
+            if (rc != DL_OK) return rc;
+            for (int m = 0; m < nm; ++m) advance(b->mem[m], 1);
+            left -= 1;
+        }
+    }
     return DL_OK;
 }
 

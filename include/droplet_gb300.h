@@ -203,6 +203,38 @@ int dl_get_option(dl_handle* h, const char* key, int64_t* value);
 /* Copy the last error message of the handle into buf (NUL-terminated). */
 int dl_last_error(dl_handle* h, char* buf, int buflen);
 
+/* ---- batched ensembles -------------------------------------------------------
+ * The reference runs ensemble members either as Nxall*Nzall replica groups of
+ * MPI ranks (MPI_Comm_Split, program/lbm_omp_drop.f90:149-166) or as a
+ * sequential loop over cases (DO case_num, program/lbm_drop_iht_xy_many.f90:1211).
+ * Here the members (each its own domain size and parameters, one common form
+ * FP32 or FP16, one common LES setting and force mode) step together: every
+ * step is one persistent launch over all members' tiles, and pairs of steps
+ * are replayed from a captured CUDA graph. */
+typedef struct dl_batch dl_batch;
+
+/* params[m] and dims[3*m .. 3*m+2] = nx, ny, nz of member m. */
+int dl_batch_create(const dl_params* params, const int* dims, int nmembers, int form, dl_batch** out);
+
+/* The handle of member m, for dl_set_fields, dl_init_equilibrium,
+ * dl_set_force, dl_get_fields, dl_reduce, ... (owned by the batch; do not
+ * dl_destroy it; do not dl_step it on its own). */
+int dl_batch_member(dl_batch* b, int m, dl_handle** member);
+
+/* Run every member's work on this cudaStream_t. */
+int dl_batch_set_stream(dl_batch* b, void* cuda_stream);
+
+/* Advance every member by nsteps steps. Launch accounting (dl_profile) is
+ * recorded on member 0's handle. */
+int dl_batch_step(dl_batch* b, int nsteps);
+
+/* Knobs: "lz" z planes per work item; "blocks_per_sm" persistent blocks per
+ * SM (1 or 2); "graph" 1 = replay step pairs from a CUDA graph. */
+int dl_batch_set_option(dl_batch* b, const char* key, int64_t value);
+int dl_batch_get_option(dl_batch* b, const char* key, int64_t* value);
+
+int dl_batch_destroy(dl_batch* b);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,111 @@
+"""Differentiable PyTorch restatement of the droplet step. TEST INFRASTRUCTURE ONLY.
+
+Used as the "plain PyTorch autodiff reference" for the hand-written adjoint:
+the same physics as the C oracle (program/lbm_drop_xy.f90:421-666 with the
+moving-wall bounce-back of prototype_program/two-phase/drop8_mpi.f90:642-674),
+written with torch.roll so that autograd differentiates it, in FP64. It does
+not follow the reference's evaluation order (it is not a parity restatement);
+its job is gradients.
+
+Fields have shape (nz, ny, nx); populations (15, nz, ny, nx).
+"""
+from __future__ import annotations
+
+import torch
+
+CX = (0, 1, 0, 0, -1, 0, 0, 1, -1, 1, 1, -1, 1, -1, -1)
+CY = (0, 0, 1, 0, 0, -1, 0, 1, 1, -1, 1, -1, -1, 1, -1)
+CZ = (0, 0, 0, 1, 0, 0, -1, 1, 1, 1, -1, -1, -1, -1, 1)
+E = [2.0 / 9.0] + [1.0 / 9.0] * 6 + [1.0 / 72.0] * 8
+H = [1.0] + [0.0] * 14
+F = [-7.0 / 3.0] + [1.0 / 3.0] * 6 + [1.0 / 24.0] * 8
+BOT = ((3, 6), (7, 11), (8, 12), (9, 13), (14, 10))   # (incoming, source) at z = 0
+TOP = ((6, 3), (10, 14), (11, 7), (12, 8), (13, 9))   # at z = nz - 1
+
+
+def nb(a, i, sign=+1):
+    """a at x + sign * c_i (periodic)."""
+    return torch.roll(a, shifts=(-sign * CZ[i], -sign * CY[i], -sign * CX[i]), dims=(0, 1, 2))
+
+
+def equilibria(P, phi, u, p, kf, kg):
+    """feq_i, geq_i (lists of 15 fields) from phi, u = (u1, u2, u3), p."""
+    lap = -14.0 * phi
+    for i in range(1, 15):
+        lap = lap + nb(phi, i)
+    lap = lap / (5.0 * P.ds * P.ds)
+    grad = []
+    for al in range(3):
+        s = torch.zeros_like(phi)
+        for i in range(1, 15):
+            c = (CX, CY, CZ)[al][i]
+            if c:
+                s = s + c * nb(phi, i)
+        grad.append(s / (10.0 * P.ds))
+    gsq = grad[0] ** 2 + grad[1] ** 2 + grad[2] ** 2
+    p0 = phi * P.T / (1.0 - P.b * phi) - P.a * phi * phi
+    A = p0 - kf * phi * lap - kf / 6.0 * gsq
+    usq = u[0] ** 2 + u[1] ** 2 + u[2] ** 2
+    feq, geq = [], []
+    for i in range(15):
+        c = (CX[i], CY[i], CZ[i])
+        cu = c[0] * u[0] + c[1] * u[1] + c[2] * u[2]
+        cg = c[0] * grad[0] + c[1] * grad[1] + c[2] * grad[2]
+        cGc = 4.5 * cg * cg - 1.5 * (c[0] ** 2 + c[1] ** 2 + c[2] ** 2) * gsq
+        feq.append(H[i] * phi + F[i] * A + 3.0 * E[i] * phi * cu + E[i] * kf * cGc)
+        geq.append(E[i] * (3.0 * p + 3.0 * cu + 4.5 * cu * cu - 1.5 * usq) + E[i] * kg * cGc)
+    return feq, geq
+
+
+def moments(f, g):
+    phi = sum(f)
+    p = sum(g) / 3.0
+    u = [sum(c[i] * g[i] for i in range(15) if c[i]) for c in (CX, CY, CZ)]
+    return phi, u, p
+
+
+def step(P, f, g, kf, kg, tauf, U, taug):
+    """One time step with constant tau_g (viscosity ratio 1). U: top-wall
+    x velocity (tensor); the bottom wall moves with -U."""
+    phi, u, p = moments(f, g)
+    feq, geq = equilibria(P, phi, u, p, kf, kg)
+    fn = [nb(f[i] - (f[i] - feq[i]) / tauf, i, -1) for i in range(15)]
+    gn = [nb(g[i] - (g[i] - geq[i]) / taug, i, -1) for i in range(15)]
+    if P.walls:
+        Uv = (U, 0.0, 0.0)
+        gb = list(gn)
+        for i, j in BOT:
+            w = 6.0 * E[j] * ((-Uv[0]) * CX[j] + (-Uv[1]) * CY[j] + (-Uv[2]) * CZ[j])
+            gb[i] = torch.cat([(gn[j][:1] - w), gn[i][1:]], dim=0)
+        for i, j in TOP:
+            w = 6.0 * E[j] * (Uv[0] * CX[j] + Uv[1] * CY[j] + Uv[2] * CZ[j])
+            gb[i] = torch.cat([gn[i][:-1], (gn[j][-1:] - w)], dim=0)
+        gn = gb
+    return fn, gn
+
+
+def deformation(P, phi):
+    """D from the covariance of w = (phi - phi1)/(phi2 - phi1)."""
+    nz, ny, nx = phi.shape
+    w = (phi - P.phi1) / (P.phi2 - P.phi1)
+    z, y, x = torch.meshgrid(torch.arange(nz, dtype=phi.dtype), torch.arange(ny, dtype=phi.dtype),
+                             torch.arange(nx, dtype=phi.dtype), indexing="ij")
+    X = torch.stack([x, y, z]).reshape(3, -1)
+    wf = w.reshape(-1)
+    W = wf.sum()
+    m = (X * wf).sum(dim=1) / W
+    S = (X * wf) @ X.T / W
+    C = S - torch.outer(m, m)
+    lam = torch.linalg.eigvalsh(C)
+    a, b = torch.sqrt(lam[-1]), torch.sqrt(lam[0])
+    return (a - b) / (a + b)
+
+
+def run_loss(P, phi0, u0, p0, kf, kg, tauf, U, taug, nsteps):
+    """Initialise at equilibrium from (phi0, u0, p0) and return D after nsteps."""
+    feq, geq = equilibria(P, phi0, u0, p0, kf, kg)
+    f, g = feq, geq
+    for _ in range(nsteps):
+        f, g = step(P, f, g, kf, kg, tauf, U, taug)
+    phi, _, _ = moments(f, g)
+    return deformation(P, phi)

@@ -1,0 +1,72 @@
+"""Batched ensembles: one persistent launch per step over members of uneven
+sizes and parameters must give each member the result it gets when stepped on
+its own (bitwise without spectral forcing, whose FP64 accumulation order is
+not fixed; within FP32 rounding with it)."""
+import numpy as np
+import pytest
+
+from droplet_gb300 import Params, init_fields
+from droplet_gb300 import _abi
+from droplet_gb300.ensemble import Ensemble
+from droplet_gb300.solver import Droplet, FORM_FP32, FORM_FP16
+
+pytestmark = pytest.mark.gpu
+
+SHAPES = [(40, 20, 16), (32, 32, 24), (48, 16, 12), (24, 24, 24)]
+
+
+def member_case(m, shape, spectral, les):
+    nx, ny, nz = shape
+    P = Params.lbm_drop_xy().replace(tauf=0.8, nu1=0.1, nu2=0.1, kappag=1e-3 * (1 + m))
+    if les:
+        P = P.replace(les=True, Cs=0.1, delta=1.0)
+    if spectral:
+        P = P.replace(eps=1e-6, kc=3)
+    rng = np.random.default_rng(100 + m)
+    phi = init_fields.tanh_droplets(shape, P, [(nx / 2 + m, ny / 2, nz / 2)], [min(shape) / 4], width=1.5)
+    u = [0.01 * rng.standard_normal((nz, ny, nx)) for _ in range(3)]
+    return P, init_fields.fields(phi, *u)
+
+
+def start(sim, f, spectral):
+    sim.set_fields(**f)
+    sim.init_equilibrium()
+    sim.set_force(_abi.DL_FORCE_SPECTRAL if spectral else _abi.DL_FORCE_NONE)
+
+
+@pytest.mark.parametrize("form", [FORM_FP32, FORM_FP16])
+@pytest.mark.parametrize("spectral,les,graph,steps", [(False, False, 1, 7), (False, True, 0, 6),
+                                                      (True, True, 1, 9)])
+def test_ensemble_matches_members_stepped_alone(form, spectral, les, graph, steps):
+    cases = [member_case(m, s, spectral, les) for m, s in enumerate(SHAPES)]
+    ens = Ensemble([c[0] for c in cases], SHAPES, form)
+    ens.set_option("graph", graph)
+    ens.set_option("lz", 8)
+    for mem, (P, f) in zip(ens.members, cases):
+        start(mem, f, spectral)
+    ens.step(steps)
+    for m, (mem, (P, f)) in enumerate(zip(ens.members, cases)):
+        solo = Droplet(P, SHAPES[m], form)
+        solo.set_option("lz", 8)
+        start(solo, f, spectral)
+        solo.step(steps)
+        a, b = mem.get_fields(), solo.get_fields()
+        assert mem.step_count == steps
+        for k in ("phi", "u1", "u2", "u3", "p"):
+            if spectral:
+                assert np.abs(a[k] - b[k]).max() <= 1e-5 * max(1.0, np.abs(b[k]).max()), (m, k)
+            else:
+                assert np.array_equal(a[k], b[k]), (m, k, np.abs(a[k] - b[k]).max())
+        assert mem.reduce()["nan_flag"] == 0
+
+
+def test_ensemble_options_and_state_checks():
+    cases = [member_case(m, s, False, False) for m, s in enumerate(SHAPES[:2])]
+    ens = Ensemble([c[0] for c in cases], SHAPES[:2], FORM_FP32)
+    for opt, val in (("lz", 4), ("blocks_per_sm", 1), ("graph", 0)):
+        ens.set_option(opt, val)
+        assert ens.get_option(opt) == val
+    from droplet_gb300 import DropletError
+
+    with pytest.raises(DropletError):
+        ens.step(1)  # members not initialised
