@@ -428,6 +428,46 @@ def run_ensemble(args):
     return 0
 
 
+def run_adjoint(args):
+    """config5: forward and reverse (hand-written adjoint, sqrt(N) checkpoints)
+    of the 96^3 shear droplet; reports the adjoint/forward time ratio."""
+    import torch
+    from droplet_gb300 import configs
+    from droplet_gb300.adjoint import CheckpointedRun
+
+    torch.cuda.set_device(0)
+    w = configs.config5()
+    nsteps = args.steps if args.steps else w.steps
+    f = w.fields
+    run = CheckpointedRun(w.params, w.shape, (f["u1"], f["u2"], f["u3"]), f["p"], nsteps)
+    run.forward(f["phi"])  # warm-up pass (builds, allocates)
+    run.backward()
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    time.sleep(0.3)
+    D = run.forward(f["phi"])
+    g = run.backward()
+    clk = clocks.stop()
+    run.close()
+    N = w.n_sites
+    fwd, bwd = run.timing.forward_s, run.timing.backward_s
+    value = N * nsteps / fwd / 1e6
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": 1, "steps": nsteps, "warmup": 1,
+        "ms_per_step": round(fwd * 1e3 / nsteps, 5), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": w.name + " adjoint", "form": "fp32", "sites": N,
+                   "adjoint_over_forward": round(bwd / fwd, 3), "forward_s": round(fwd, 4),
+                   "backward_s": round(bwd, 4), "checkpoint_every": run.S, "loss_D": D,
+                   "grads": {k: v for k, v in g.items() if k != "dphi0"},
+                   "note": "forward = n steps with checkpoint saves + field download; backward = segment "
+                           "recomputation + reverse steps + reverse of the initial equilibrium"},
+        "roofline": None, "cpu_baseline": None, "e2e": None, "clocks": clk, "gpu_launches": None,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -447,6 +487,8 @@ def main():
         return run_reference(args)
     if args.workload == "config4":
         return run_ensemble(args)
+    if args.workload == "config5":
+        return run_adjoint(args)
     return run_ours(args)
 
 

@@ -154,6 +154,22 @@ def declare(lib: C.CDLL, prefix: str) -> None:
         lib.dl_set_option.restype = C.c_int
         lib.dl_get_option.argtypes = [h, C.c_char_p, C.POINTER(C.c_int64)]
         lib.dl_get_option.restype = C.c_int
+        lib.dl_label_droplets.argtypes = [h, C.c_int, _vp, C.POINTER(C.c_int64), _dp, C.c_int64]
+        lib.dl_label_droplets.restype = C.c_int
+        lib.dl_state_floats.argtypes = [h, C.POINTER(C.c_int64)]
+        lib.dl_state_floats.restype = C.c_int
+        lib.dl_save_state.argtypes = [h, _vp]
+        lib.dl_save_state.restype = C.c_int
+        lib.dl_load_state.argtypes = [h, _vp]
+        lib.dl_load_state.restype = C.c_int
+        lib.dl_adjoint_begin.argtypes = [h, _vp]
+        lib.dl_adjoint_begin.restype = C.c_int
+        lib.dl_adjoint_step.argtypes = [h, _vp, C.c_int64]
+        lib.dl_adjoint_step.restype = C.c_int
+        lib.dl_adjoint_init.argtypes = [h, _vp, _vp]
+        lib.dl_adjoint_init.restype = C.c_int
+        lib.dl_adjoint_grads.argtypes = [h, _dp]
+        lib.dl_adjoint_grads.restype = C.c_int
         lib.dl_batch_create.argtypes = [C.POINTER(DLParams), C.POINTER(C.c_int), C.c_int, C.c_int, C.POINTER(_vp)]
         lib.dl_batch_create.restype = C.c_int
         lib.dl_batch_member.argtypes = [_vp, C.c_int, C.POINTER(_vp)]
@@ -203,6 +219,14 @@ HEADER_SYMBOLS = [
     "dl_profile_read",
     "dl_set_option",
     "dl_get_option",
+    "dl_label_droplets",
+    "dl_state_floats",
+    "dl_save_state",
+    "dl_load_state",
+    "dl_adjoint_begin",
+    "dl_adjoint_step",
+    "dl_adjoint_init",
+    "dl_adjoint_grads",
     "dl_batch_create",
     "dl_batch_member",
     "dl_batch_set_stream",

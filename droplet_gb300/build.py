@@ -43,6 +43,8 @@ SOURCES = {
     "layout.cu": EXACT,
     "reduce.cu": EXACT,
     "step_fast.cu": FAST,
+    "adjoint.cu": FAST,
+    "labels.cu": FAST,
 }
 
 

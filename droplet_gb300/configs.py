@@ -155,4 +155,10 @@ def config4(n_members: int = 64, seed: int = 4):
     return ensemble_members(n_members=n_members, seed=seed)
 
 
-WORKLOADS = {"config1": config1, "config2": config2, "config3": config3, "config4": config4}
+def config5(n: int = 96) -> Workload:
+    """Adjoint workload: 96^3 shear droplet (config-1 physics), R = 18,
+    walls +-0.04, FP32, 500 steps; loss = deformation at the final step."""
+    return shear_droplet(n=n, radius=18.0 * n / 96.0, U=0.04, form=_abi.DL_FORM_FP32, steps=500)
+
+
+WORKLOADS = {"config1": config1, "config2": config2, "config3": config3, "config4": config4, "config5": config5}

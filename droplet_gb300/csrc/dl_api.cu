@@ -179,9 +179,11 @@ int dl_destroy(dl_handle* h) {
     if (h->stream) cudaStreamSynchronize(h->stream);
     fp64_free(h);
     fast_free(h);
+    adjoint_free(h);
     spectral_free(h);
     cudaFree(h->d_state);
     cudaFree(h->d_diag);
+    cudaFree(h->lbl_buf);
     prof_release(h);
     delete h;
     return DL_OK;
@@ -214,6 +216,68 @@ int dl_profile_read(dl_handle* h, dl_profile_stats* out) {
     h->prof_n = 0;
     h->launches = 0;
     return DL_OK;
+}
+
+int dl_label_droplets(dl_handle* h, int connectivity, int32_t* labels, int64_t* ndrops, double* volumes,
+                      int64_t max_volumes) {
+    if (!h || !ndrops || (max_volumes > 0 && !volumes) || max_volumes < 0) return DL_ERR_ARG;
+    long long n = 0;
+    int rc = label_droplets(h, connectivity, (int*)labels, &n, volumes, (long long)max_volumes);
+    *ndrops = (int64_t)n;
+    return rc;
+}
+
+int dl_state_floats(dl_handle* h, int64_t* n) {
+    if (!h || !n) return DL_ERR_ARG;
+    if (h->form != DL_FORM_FP32) return set_error(h, DL_ERR_UNSUPPORTED, "device state export is for the FP32 form");
+    *n = (int64_t)35 * (int64_t)h->N;
+    return DL_OK;
+}
+
+int dl_save_state(dl_handle* h, void* d_dst) {
+    if (!h || !d_dst) return DL_ERR_ARG;
+    if (h->form != DL_FORM_FP32) return set_error(h, DL_ERR_UNSUPPORTED, "device state export is for the FP32 form");
+    const size_t N = h->N;
+    float* d = (float*)d_dst;
+    DL_CUDA(h, cudaMemcpyAsync(d, h->fs[h->cur], sizeof(float) * Q * N, cudaMemcpyDeviceToDevice, h->stream));
+    DL_CUDA(h, cudaMemcpyAsync(d + Q * N, h->gs[h->cur], sizeof(float) * Q * N, cudaMemcpyDeviceToDevice, h->stream));
+    DL_CUDA(h, cudaMemcpyAsync(d + 2 * Q * N, h->mac32[h->cur], sizeof(float) * 5 * N, cudaMemcpyDeviceToDevice,
+                               h->stream));
+    return DL_OK;
+}
+
+int dl_load_state(dl_handle* h, const void* d_src) {
+    if (!h || !d_src) return DL_ERR_ARG;
+    if (h->form != DL_FORM_FP32) return set_error(h, DL_ERR_UNSUPPORTED, "device state import is for the FP32 form");
+    const size_t N = h->N;
+    const float* d = (const float*)d_src;
+    DL_CUDA(h, cudaMemcpyAsync(h->fs[h->cur], d, sizeof(float) * Q * N, cudaMemcpyDeviceToDevice, h->stream));
+    DL_CUDA(h, cudaMemcpyAsync(h->gs[h->cur], d + Q * N, sizeof(float) * Q * N, cudaMemcpyDeviceToDevice, h->stream));
+    DL_CUDA(h, cudaMemcpyAsync(h->mac32[h->cur], d + 2 * Q * N, sizeof(float) * 5 * N, cudaMemcpyDeviceToDevice,
+                               h->stream));
+    h->fields_set = true;
+    h->eq_init = true;
+    return DL_OK;
+}
+
+int dl_adjoint_begin(dl_handle* h, const float* d_dloss_dphi) {
+    if (!h || !d_dloss_dphi) return DL_ERR_ARG;
+    return adjoint_begin(h, d_dloss_dphi);
+}
+
+int dl_adjoint_step(dl_handle* h, const void* d_state_before, int64_t step) {
+    if (!h || !d_state_before || step < 1) return DL_ERR_ARG;
+    return adjoint_step(h, (const float*)d_state_before, (long long)step);
+}
+
+int dl_adjoint_init(dl_handle* h, const void* d_state0, float* d_dloss_dphi0) {
+    if (!h || !d_state0 || !d_dloss_dphi0) return DL_ERR_ARG;
+    return adjoint_init(h, (const float*)d_state0, d_dloss_dphi0);
+}
+
+int dl_adjoint_grads(dl_handle* h, double* grads) {
+    if (!h || !grads) return DL_ERR_ARG;
+    return adjoint_grads(h, grads);
 }
 
 int dl_set_option(dl_handle* h, const char* key, int64_t value) {

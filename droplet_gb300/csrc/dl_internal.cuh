@@ -141,6 +141,15 @@ struct dl_handle {
     double* d_diag;          // diagnostics partial sums
     int diag_blocks;
 
+    // labelling scratch (labels.cu)
+    int* lbl_buf;
+
+    // adjoint (adjoint.cu)
+    float* adj_lam[2];       // [30][N] adjoints of f and g
+    float* adj_aux;          // [9][N]
+    double* adj_grads;       // [4]
+    int adj_cur;
+
     // launch accounting (dl_profile)
     int64_t launches;
     int prof_on;
@@ -182,6 +191,15 @@ void batch_destroy(void* b);
 int batch_step(void* b, int nsteps);
 int batch_set_option(void* b, const char* key, long long v);
 int batch_get_option(void* b, const char* key, long long* v);
+// droplet labelling (labels.cu)
+int label_droplets(dl_handle* h, int conn, int* labels_host, long long* ndrops, double* volumes, long long maxv);
+// adjoint of the FP32 step (adjoint.cu)
+int adjoint_check(dl_handle* h);
+void adjoint_free(dl_handle* h);
+int adjoint_begin(dl_handle* h, const float* d_lphi);
+int adjoint_step(dl_handle* h, const float* d_state, long long step);
+int adjoint_init(dl_handle* h, const float* d_state0, float* d_lphi0);
+int adjoint_grads(dl_handle* h, double* out4);
 // transposes (layout.cu)
 int soa_to_aos(dl_handle* h, const double* d_soa, double* d_aos);
 int aos_to_soa(dl_handle* h, const double* d_aos, double* d_soa);

@@ -198,6 +198,16 @@ class Droplet(_HandleAPI):
         self._call("reduce", C.byref(d))
         return d.as_dict()
 
+    def label_droplets(self, connectivity: int = 14, labels: bool = False, max_volumes: int = 100000):
+        """Droplets = periodic connected components of phi >= (phi1+phi2)/2.
+        Returns (volumes sorted decreasing, labels array or None)."""
+        n = C.c_int64()
+        vols = np.zeros(max_volumes, dtype=np.float64)
+        lab = np.empty(self.shape3, dtype=np.int32) if labels else None
+        self._call("label_droplets", int(connectivity), lab.ctypes.data_as(C.c_void_p) if labels else None,
+                   C.byref(n), _ptr(vols), C.c_int64(max_volumes))
+        return vols[: min(int(n.value), max_volumes)].copy(), lab
+
     def profile(self, enable: bool = True):
         """Bracket every launch with CUDA events (and reset the counters)."""
         self._call("profile", 1 if enable else 0)

@@ -203,6 +203,45 @@ int dl_get_option(dl_handle* h, const char* key, int64_t* value);
 /* Copy the last error message of the handle into buf (NUL-terminated). */
 int dl_last_error(dl_handle* h, char* buf, int buflen);
 
+/* Connected components of the sites with phi >= (phi1 + phi2)/2 on the
+ * periodic lattice (droplet labelling of program/percolation.f90:108-295,
+ * made complete across the periodic boundaries). connectivity: 6 (faces),
+ * 14 (faces + xz and yz edges, the reference's neighbour set made symmetric),
+ * 18 (faces + edges) or 26. Writes the number of droplets, up to max_volumes
+ * volumes (site counts, decreasing) and, if labels is not NULL, nx*ny*nz
+ * labels (0 = continuous phase, k = k-th largest droplet, x fastest). */
+int dl_label_droplets(dl_handle* h, int connectivity, int32_t* labels, int64_t* ndrops, double* volumes,
+                      int64_t max_volumes);
+
+/* ---- device state and the hand-written adjoint (FP32 form) ---------------------
+ * No reference counterpart: the reference has no derivatives. The adjoint runs
+ * the reverse of dl_step for a loss on the final phi, with the caller driving
+ * checkpointing: save states with dl_save_state (device memory of
+ * dl_state_floats floats), recompute segments with dl_load_state + dl_step,
+ * and walk them backwards with dl_adjoint_step. It covers the shear-droplet
+ * physics (walls, static force, viscosity ratio 1, no LES / spectral force). */
+
+/* Number of FP32 values of one device state (populations and fields). */
+int dl_state_floats(dl_handle* h, int64_t* n);
+
+/* Copy the current state to / from caller-owned device memory. */
+int dl_save_state(dl_handle* h, void* d_dst);
+int dl_load_state(dl_handle* h, const void* d_src);
+
+/* Start the reverse pass from dLoss/dphi of the final fields (device, N floats). */
+int dl_adjoint_begin(dl_handle* h, const float* d_dloss_dphi);
+
+/* Reverse of time step `step` (1-based); d_state_before is the state saved
+ * before that step. */
+int dl_adjoint_step(dl_handle* h, const void* d_state_before, int64_t step);
+
+/* Reverse of dl_init_equilibrium from the initial state: writes dLoss/dphi0. */
+int dl_adjoint_init(dl_handle* h, const void* d_state0, float* d_dloss_dphi0);
+
+/* Accumulated parameter gradients: dLoss/dkappaf, dLoss/dkappag,
+ * dLoss/dtauf, dLoss/dU (top-wall x velocity; bottom = -U). */
+int dl_adjoint_grads(dl_handle* h, double* grads4);
+
 /* ---- batched ensembles -------------------------------------------------------
  * The reference runs ensemble members either as Nxall*Nzall replica groups of
  * MPI ranks (MPI_Comm_Split, program/lbm_omp_drop.f90:149-166) or as a
