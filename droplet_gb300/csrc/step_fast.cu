@@ -1321,6 +1321,7 @@ struct BatchImpl {
     int lz, bps, use_graph;
     int sms;
     cudaStream_t stream;
+    cudaStream_t cap_stream;  // owned stream the graph is captured on (the legacy default stream cannot capture)
     cudaGraphExec_t gexec;
     int graph_ok;
     int built_parity;       // member parity the tables were built at (-1: rebuild)
@@ -1400,6 +1401,7 @@ void batch_destroy(void* p) {
     BatchImpl* b = (BatchImpl*)p;
     if (!b) return;
     if (b->graph_ok) cudaGraphExecDestroy(b->gexec);
+    if (b->cap_stream) cudaStreamDestroy(b->cap_stream);
     cudaFree(b->d_table);
     cudaFree(b->d_items);
     cudaFree(b->d_nblk);
@@ -1497,11 +1499,20 @@ static int batch_build(BatchImpl* b) {
         b->graph_ok = 0;
     }
     if (b->use_graph) {
+        // capture on the batch's own stream, replay on the caller's stream
+        if (!b->cap_stream) DL_CUDA(h0, cudaStreamCreateWithFlags(&b->cap_stream, cudaStreamNonBlocking));
         cudaGraph_t g;
-        DL_CUDA(h0, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+        const cudaStream_t user = b->stream;
+        b->stream = b->cap_stream;
+        cudaError_t e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeRelaxed);
+        if (e != cudaSuccess) {
+            b->stream = user;
+            return check_cuda(h0, e, "cudaStreamBeginCapture");
+        }
         int rc = launch_batched(b, 0);
         if (rc == DL_OK) rc = launch_batched(b, 1);
-        cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+        e = cudaStreamEndCapture(b->stream, &g);
+        b->stream = user;
         if (rc != DL_OK) return rc;
         DL_CUDA(h0, e);
         e = cudaGraphInstantiate(&b->gexec, g, 0);
