@@ -38,6 +38,9 @@ DL_FORCE_SPECTRAL = 2
 DL_VISC_MINMAX = 0
 DL_VISC_FIXED = 1
 
+DL_REDUCE_STATIC_MAX_BLOCKS = 1216
+DL_REDUCE_STATIC_SCRATCH_BYTES = 253144
+
 
 class DLParams(C.Structure):
     _fields_ = [
@@ -142,6 +145,8 @@ def declare(lib: C.CDLL, prefix: str) -> None:
         lib.dl_set_stream.restype = C.c_int
         lib.dl_reduce.argtypes = [h, C.POINTER(DLDiag)]
         lib.dl_reduce.restype = C.c_int
+        lib.dl_reduce_static.argtypes = [h, C.c_int, C.POINTER(DLDiag)]
+        lib.dl_reduce_static.restype = C.c_int
         lib.dl_sync.argtypes = [h]
         lib.dl_sync.restype = C.c_int
         lib.dl_last_error.argtypes = [h, C.c_char_p, C.c_int]
@@ -213,6 +218,7 @@ HEADER_SYMBOLS = [
     "dl_get_step",
     "dl_get_minmax",
     "dl_reduce",
+    "dl_reduce_static",
     "dl_sync",
     "dl_last_error",
     "dl_profile",

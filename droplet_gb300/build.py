@@ -42,6 +42,7 @@ SOURCES = {
     "spectral.cu": EXACT,
     "layout.cu": EXACT,
     "reduce.cu": EXACT,
+    "reduce_static.cu": EXACT,
     "step_fast.cu": FAST,
     "adjoint.cu": FAST,
     "labels.cu": FAST,

@@ -1,0 +1,310 @@
+// reduce_static.cu -- dl_reduce_static: the whole-domain diagnostics of
+// dl_reduce (same sums, same formulas) in a single launch whose working
+// memory is one fixed array compiled into this library. The call allocates
+// no device memory: no cudaMalloc, no cudaFree, no allocating library
+// routine, and it skips the launch-event profiling (whose event pool may
+// grow). It serves callers that must not allocate once a run is set up,
+// for instance a host program that reserves nearly all of the GPU's memory
+// for its lattices up front and would fail (or have to give memory back) on
+// the few-kilobyte buffer that dl_reduce takes on its first call, or a
+// monitoring thread that must not enter the device allocator while other
+// threads keep stepping.
+//
+// The array is shared by every handle on a device. Calls that overlap in
+// time on one device (from two streams, two handles or two host threads)
+// race on it and give wrong sums: the caller serialises them.
+#include "dl_internal.cuh"
+
+#include <atomic>
+#include <string.h>
+
+namespace dl {
+
+constexpr int RS_NSUM = 24;  // sums, then min, max (the dl_reduce set)
+constexpr int RS_NPART = RS_NSUM + 2;
+constexpr int RS_THREADS = 256;
+constexpr int RS_MAX_BLOCKS = DL_REDUCE_STATIC_MAX_BLOCKS;
+constexpr int RS_DEFAULT_BLOCKS = 304;  // 2 x 152 SMs
+constexpr int RS_SEGS = 8;              // block-order segments of the final sum
+
+// Layout, in doubles: [0, RS_MAX_BLOCKS * RS_NPART) per-block partials,
+// then RS_NPART results, then one 64-bit arrival counter. 253,144 bytes.
+// Nothing in the partials or the results has to start at zero: every call
+// writes them before it reads them. The counter must be zero when a call
+// starts: the array is zero when the library is loaded, and the last block
+// of every call puts the counter back to zero.
+constexpr size_t RS_WORDS = (size_t)RS_MAX_BLOCKS * RS_NPART + RS_NPART + 1;
+static __device__ __align__(256) double g_reduce_scratch[RS_WORDS];
+
+static_assert(RS_WORDS * sizeof(double) == DL_REDUCE_STATIC_SCRATCH_BYTES, "scratch size and header disagree");
+
+struct RsArgs {
+    int nx, ny, nz;
+    long long N;
+    double phi1, phi2, nu1, dnu, graddiv;
+    double phi_off, p_off;  // stored phi and p are phi - phi_off, p - p_off
+};
+
+__device__ __forceinline__ long long rs_wrap(int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); }
+
+// Neumaier step: (s, c) += v
+__device__ __forceinline__ void rs_add(double& s, double& c, double v) {
+    const double t = s + v;
+    if (fabs(s) >= fabs(v)) c += (s - t) + v;
+    else c += (v - t) + s;
+    s = t;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(RS_THREADS) reduce_static_kernel(const T* __restrict__ mac, const RsArgs a,
+                                                                   double* __restrict__ scratch) {
+    double* part = scratch;
+    double* result = scratch + (size_t)RS_MAX_BLOCKS * RS_NPART;
+    unsigned long long* arrivals = reinterpret_cast<unsigned long long*>(result + RS_NPART);
+
+    double acc[RS_NSUM];
+#pragma unroll
+    for (int k = 0; k < RS_NSUM; ++k) acc[k] = 0.0;
+    double vmin = INFINITY, vmax = -INFINITY;
+    const long long N = a.N;
+    const double inv = 1.0 / (a.phi2 - a.phi1);
+    const double mid = 0.5 * (a.phi1 + a.phi2);
+    for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < N; s += (long long)gridDim.x * blockDim.x) {
+        const long long row = s / a.nx;
+        const int x = (int)(s - row * a.nx);
+        const int z = (int)(row / a.ny);
+        const int y = (int)(row - (long long)z * a.ny);
+        const double ph = a.phi_off + (double)mac[s];
+        const double u1 = (double)mac[N + s], u2 = (double)mac[2 * N + s], u3 = (double)mac[3 * N + s];
+        const double p = a.p_off + (double)mac[4 * N + s];
+        // du_b/dx_a with the 14-neighbour gradient stencil: gu[b + 3a]
+        double gu[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) gu[k] = 0.0;
+#pragma unroll
+        for (int i = 1; i < Q; ++i) {
+            const long long nb = rs_wrap(x + cx(i), a.nx) +
+                                 (long long)a.nx * (rs_wrap(y + cy(i), a.ny) + (long long)a.ny * rs_wrap(z + cz(i), a.nz));
+            const double v[3] = {(double)mac[N + nb], (double)mac[2 * N + nb], (double)mac[3 * N + nb]};
+            const double c[3] = {(double)cx(i), (double)cy(i), (double)cz(i)};
+#pragma unroll
+            for (int al = 0; al < 3; ++al)
+#pragma unroll
+                for (int be = 0; be < 3; ++be) gu[be + 3 * al] += c[al] * v[be];
+        }
+        double ss = 0.0;
+#pragma unroll
+        for (int be = 0; be < 3; ++be)
+#pragma unroll
+            for (int al = 0; al < 3; ++al) {
+                const double st = 0.5 * (gu[al + 3 * be] + gu[be + 3 * al]) / a.graddiv;
+                ss += st * st;
+            }
+        const double w = (ph - a.phi1) * inv;
+        const double nu = a.nu1 + w * a.dnu;
+        acc[0] += ph;
+        acc[1] += p;
+        acc[2] += u1;
+        acc[3] += u2;
+        acc[4] += u3;
+        acc[5] += 0.5 * (u1 * u1 + u2 * u2 + u3 * u3);
+        acc[6] += 2.0 * nu * ss;
+        acc[7] += (ph > mid) ? 1.0 : 0.0;
+        acc[8] += w;
+        if (w > 0.95) {
+            acc[9] += p;
+            acc[10] += 1.0;
+        }
+        if (w < 0.05) {
+            acc[11] += p;
+            acc[12] += 1.0;
+        }
+        const double X = (double)x, Y = (double)y, Z = (double)z;
+        acc[13] += w;
+        acc[14] += w * X;
+        acc[15] += w * Y;
+        acc[16] += w * Z;
+        acc[17] += w * X * X;
+        acc[18] += w * Y * Y;
+        acc[19] += w * Z * Z;
+        acc[20] += w * X * Y;
+        acc[21] += w * X * Z;
+        acc[22] += w * Y * Z;
+        acc[23] += (ph == ph && isfinite(ph)) ? 0.0 : 1.0;
+        if (ph == ph) {
+            vmin = fmin(vmin, ph);
+            vmax = fmax(vmax, ph);
+        }
+    }
+
+    // block partials: warp shuffles, then one row per warp in shared memory
+    __shared__ double sh[RS_THREADS / 32][RS_NPART];
+    __shared__ double seg_s[RS_NPART][RS_SEGS], seg_c[RS_NPART][RS_SEGS];
+    __shared__ bool is_last;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < RS_NSUM; ++k) {
+        double v = acc[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) sh[warp][k] = v;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        vmin = fmin(vmin, __shfl_xor_sync(0xffffffffu, vmin, o));
+        vmax = fmax(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
+    }
+    if (lane == 0) {
+        sh[warp][RS_NSUM] = vmin;
+        sh[warp][RS_NSUM + 1] = vmax;
+    }
+    __syncthreads();
+    if (threadIdx.x < RS_NPART) {
+        const int k = threadIdx.x;
+        double v = sh[0][k];
+        for (int w = 1; w < RS_THREADS / 32; ++w) {
+            if (k == RS_NSUM) v = fmin(v, sh[w][k]);
+            else if (k == RS_NSUM + 1) v = fmax(v, sh[w][k]);
+            else v += sh[w][k];
+        }
+        part[(size_t)blockIdx.x * RS_NPART + k] = v;
+        __threadfence();  // the partial is visible device-wide before this block counts itself in
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) is_last = (atomicAdd(arrivals, 1ull) == (unsigned long long)gridDim.x - 1);
+    __syncthreads();
+    if (!is_last) return;
+
+    // last block to arrive: fixed-order compensated sum over the blocks, in
+    // RS_SEGS contiguous segments, then the segments in order
+    __threadfence();
+    const int nb = (int)gridDim.x;
+    const int per = (nb + RS_SEGS - 1) / RS_SEGS;
+    if (threadIdx.x < RS_NPART * RS_SEGS) {
+        const int k = threadIdx.x / RS_SEGS, sg = threadIdx.x % RS_SEGS;
+        const int b0 = sg * per, b1 = min(nb, b0 + per);
+        double s = 0.0, c = 0.0;
+        if (k == RS_NSUM) s = INFINITY;
+        if (k == RS_NSUM + 1) s = -INFINITY;
+        for (int b = b0; b < b1; ++b) {
+            const double v = __ldcg(part + (size_t)b * RS_NPART + k);
+            if (k == RS_NSUM) s = fmin(s, v);
+            else if (k == RS_NSUM + 1) s = fmax(s, v);
+            else rs_add(s, c, v);
+        }
+        seg_s[k][sg] = s;
+        seg_c[k][sg] = c;
+    }
+    __syncthreads();
+    if (threadIdx.x < RS_NPART) {
+        const int k = threadIdx.x;
+        double s = seg_s[k][0], c = seg_c[k][0];
+        for (int sg = 1; sg < RS_SEGS; ++sg) {
+            if (k == RS_NSUM) s = fmin(s, seg_s[k][sg]);
+            else if (k == RS_NSUM + 1) s = fmax(s, seg_s[k][sg]);
+            else {
+                rs_add(s, c, seg_s[k][sg]);
+                c += seg_c[k][sg];
+            }
+        }
+        result[k] = (k >= RS_NSUM) ? s : s + c;
+    }
+    if (threadIdx.x == 0) atomicExch(arrivals, 0ull);  // ready for the next call
+}
+
+// Device address of g_reduce_scratch, looked up once per device (with that
+// device current) and kept. Concurrent first calls may both look it up; they
+// store the same value.
+constexpr int RS_MAX_DEVICES = 64;
+static std::atomic<double*> g_scratch_addr[RS_MAX_DEVICES];
+
+static int scratch_address(dl_handle* h, double** out) {
+    if (h->device < 0 || h->device >= RS_MAX_DEVICES)
+        return set_error(h, DL_ERR_UNSUPPORTED, "dl_reduce_static supports device ordinals below %d", RS_MAX_DEVICES);
+    double* p = g_scratch_addr[h->device].load(std::memory_order_acquire);
+    if (!p) {
+        void* addr = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&addr, g_reduce_scratch);
+        if (e != cudaSuccess) return check_cuda(h, e, "cudaGetSymbolAddress(g_reduce_scratch)");
+        p = static_cast<double*>(addr);
+        g_scratch_addr[h->device].store(p, std::memory_order_release);
+    }
+    *out = p;
+    return DL_OK;
+}
+
+template <typename T>
+static int reduce_static_any(dl_handle* h, const T* d_mac, double phi_off, double p_off, int nblocks, dl_diag* out) {
+    double* scratch = nullptr;
+    int rc = scratch_address(h, &scratch);
+    if (rc != DL_OK) return rc;
+    RsArgs a;
+    memset(&a, 0, sizeof(a));
+    a.nx = h->nx;
+    a.ny = h->ny;
+    a.nz = h->nz;
+    a.N = (long long)h->N;
+    a.phi1 = h->P.phi1;
+    a.phi2 = h->P.phi2;
+    a.nu1 = h->P.nu1;
+    a.dnu = h->P.nu2 - h->P.nu1;
+    a.graddiv = 10.0 * h->P.ds;
+    a.phi_off = phi_off;
+    a.p_off = p_off;
+    reduce_static_kernel<T><<<nblocks, RS_THREADS, 0, h->stream>>>(d_mac, a, scratch);
+    DL_CUDA(h, cudaGetLastError());
+    h->launches += 1;
+    double r[RS_NPART];
+    DL_CUDA(h, cudaMemcpyAsync(r, scratch + (size_t)RS_MAX_BLOCKS * RS_NPART, sizeof(r), cudaMemcpyDeviceToHost,
+                               h->stream));
+    DevState st;
+    DL_CUDA(h, cudaMemcpyAsync(&st, h->d_state, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
+    DL_CUDA(h, cudaStreamSynchronize(h->stream));
+    memset(out, 0, sizeof(*out));
+    out->phi_sum = r[0];
+    out->p_sum = r[1];
+    out->mom[0] = r[2];
+    out->mom[1] = r[3];
+    out->mom[2] = r[4];
+    out->ke = r[5];
+    out->diss = r[6];
+    out->vol_count = r[7];
+    out->vol_smooth = r[8];
+    out->p_in = r[9];
+    out->n_in = r[10];
+    out->p_out = r[11];
+    out->n_out = r[12];
+    out->w_sum = r[13];
+    for (int k = 0; k < 3; ++k) out->w_x[k] = r[14 + k];
+    for (int k = 0; k < 6; ++k) out->w_xx[k] = r[17 + k];
+    out->phi_min = r[RS_NSUM];
+    out->phi_max = r[RS_NSUM + 1];
+    out->step = h->step;
+    out->nan_flag = st.nan_flag;
+    return DL_OK;
+}
+
+}  // namespace dl
+
+extern "C" int dl_reduce_static(dl_handle* h, int nblocks, dl_diag* out) {
+    if (!h || !out) return DL_ERR_ARG;
+    if (nblocks == 0) nblocks = dl::RS_DEFAULT_BLOCKS;
+    if (nblocks < 1 || nblocks > DL_REDUCE_STATIC_MAX_BLOCKS)
+        return dl::set_error(h, DL_ERR_ARG,
+                             "dl_reduce_static: nblocks %d is outside 1..%d (the fixed scratch of %d bytes holds the "
+                             "partial sums of at most %d blocks); pass 0 for the default of %d",
+                             nblocks, DL_REDUCE_STATIC_MAX_BLOCKS, (int)DL_REDUCE_STATIC_SCRATCH_BYTES,
+                             DL_REDUCE_STATIC_MAX_BLOCKS, dl::RS_DEFAULT_BLOCKS);
+    if (!h->fields_set) return dl::set_error(h, DL_ERR_STATE, "dl_reduce_static: fields not set");
+    int prev = -1;
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    if (prev != h->device) {
+        const cudaError_t e = cudaSetDevice(h->device);
+        if (e != cudaSuccess) return dl::check_cuda(h, e, "cudaSetDevice");
+    }
+    const bool fast = h->form != DL_FORM_FP64;
+    const int rc = fast ? dl::reduce_static_any<float>(h, h->mac32[h->cur], h->P.phi1, 1.0 / 3.0, nblocks, out)
+                        : dl::reduce_static_any<double>(h, h->mac64[h->cur], 0.0, 0.0, nblocks, out);
+    if (prev >= 0 && prev != h->device) cudaSetDevice(prev);
+    return rc;
+}

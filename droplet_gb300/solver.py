@@ -198,6 +198,14 @@ class Droplet(_HandleAPI):
         self._call("reduce", C.byref(d))
         return d.as_dict()
 
+    def reduce_static(self, nblocks: int = 0) -> dict:
+        """The diagnostics of reduce() through dl_reduce_static, which
+        allocates no device memory (fixed scratch inside the library, shared
+        per device: calls on one device must not overlap)."""
+        d = _abi.DLDiag()
+        self._call("reduce_static", int(nblocks), C.byref(d))
+        return d.as_dict()
+
     def label_droplets(self, connectivity: int = 14, labels: bool = False, max_volumes: int = 100000):
         """Droplets = periodic connected components of phi >= (phi1+phi2)/2.
         Returns (volumes sorted decreasing, labels array or None)."""

@@ -181,6 +181,29 @@ int dl_get_minmax(dl_handle* h, double* phi_min, double* phi_max);
  * droplet moments of prototype_program/two-phase/drop8_mpi.f90:812-970). */
 int dl_reduce(dl_handle* h, dl_diag* out);
 
+/* dl_reduce_static: the same diagnostics as dl_reduce, for callers that must
+ * not allocate device memory once their run is set up -- a host program that
+ * has reserved nearly all of the GPU's memory for its lattices, or a
+ * monitoring thread that must not enter the device allocator while other
+ * threads step. It allocates nothing: its working memory is one fixed array
+ * of DL_REDUCE_STATIC_SCRATCH_BYTES compiled into the library, shared by
+ * every handle on a device. No counterpart in the reference.
+ *
+ * nblocks: blocks of the one reduction launch, 1..DL_REDUCE_STATIC_MAX_BLOCKS
+ * (0 = 304); larger values are rejected with DL_ERR_ARG and a message. The
+ * sums are compensated and added in a fixed order, so repeated calls on the
+ * same fields with the same nblocks return identical values; they agree with
+ * dl_reduce to rounding (the order of the final additions differs).
+ *
+ * The first call on each device looks up the array's device address (once,
+ * with that device made current for the call); make that first call before
+ * any stream capture starts on the device. Calls on one device must not
+ * overlap in time (two streams, two handles or two host threads at once):
+ * they share the array and would race. The call synchronises h's stream. */
+#define DL_REDUCE_STATIC_MAX_BLOCKS 1216
+#define DL_REDUCE_STATIC_SCRATCH_BYTES 253144
+int dl_reduce_static(dl_handle* h, int nblocks, dl_diag* out);
+
 /* Wait for all work of the handle; returns the first deferred error. */
 int dl_sync(dl_handle* h);
 
