@@ -47,13 +47,19 @@ def measured_peak_gbs():
 
 def committed_traffic(kernel: str, workload: str):
     """DRAM bytes per launch from the committed ncu summary, if one exists."""
-    p = os.path.join(ROOT, "profiles", "traffic.json")
+    p = os.path.join(ROOT, "profiles", "traffic.txt")
     try:
         with open(p) as fh:
-            d = json.load(fh)
-        return d.get(f"{kernel}:{workload}")
-    except Exception:
-        return None
+            for line in fh:
+                line = line.split("#", 1)[0].strip()
+                if "=" not in line:
+                    continue
+                key, val = (t.strip() for t in line.split("=", 1))
+                if key == f"{kernel}:{workload}":
+                    return int(val)
+    except OSError:
+        pass
+    return None
 
 
 class ClockSampler:

@@ -99,7 +99,7 @@ struct FastSpectral {
     int* d_kxoff;        // first mode of each kx
     float2* d_tw[3];     // e^{i 2 pi m / n} for x, y, z
     float2* d_fh[2];     // [3][nm] synthesis coefficients
-    double* d_acc;       // [3][nm][2] projection accumulators
+    double* d_acc;       // [16][3][nm][2] projection accumulators (copies cut atomic contention)
 };
 
 }  // namespace dl

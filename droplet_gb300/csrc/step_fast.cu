@@ -58,6 +58,7 @@ enum { F_NONE = 0, F_ARRAY = 1, F_SPECTRAL = 2 };
 constexpr int SK = 2;                 // in-kernel spectral forcing: |k_x| <= 2 (kc <= 3)
 constexpr int SNK = 2 * SK + 1;
 constexpr int SMAXM = 64;             // at most 64 band modes (two per lane)
+constexpr int SP_NREP = 16;           // copies of the projection accumulators (block b adds to copy b % 16)
 
 struct FastArgs {
     int nx, ny, nz, lz;
@@ -87,6 +88,13 @@ struct FastArgs {
     const float2* twz;
     double half_eps, invN;
 };
+
+// v within a few periods of [0, n) (plane indices z - 2 .. z + 4): no division
+__device__ __forceinline__ int wrap_near(int v, int n) {
+    while (v < 0) v += n;
+    while (v >= n) v -= n;
+    return v;
+}
 
 __device__ __forceinline__ int pmod(int v, int n) {
     v %= n;
@@ -248,13 +256,24 @@ __device__ void spectral_finalize(const FastArgs& a) {
     __shared__ double s_e[NWARP];
     __shared__ double s_coef;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nv = 6 * a.nm;  // values per accumulator copy
+    // fold the copies into copy 0 (fixed order)
+    for (int t = tid; t < nv; t += blockDim.x) {
+        double v = __ldcg(a.acc + t);
+        for (int r = 1; r < SP_NREP; ++r) {
+            v += __ldcg(a.acc + (size_t)r * nv + t);
+            a.acc[(size_t)r * nv + t] = 0.0;
+        }
+        a.acc[t] = v;
+    }
+    __syncthreads();
     double e = 0.0;
     for (int m = tid; m < a.nm; m += blockDim.x) {
         double s = 0.0;
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            const double re = __ldcg(a.acc + 2 * (c * a.nm + m)) * a.invN;
-            const double im = __ldcg(a.acc + 2 * (c * a.nm + m) + 1) * a.invN;
+            const double re = a.acc[2 * (c * a.nm + m)] * a.invN;
+            const double im = a.acc[2 * (c * a.nm + m) + 1] * a.invN;
             s += re * re + im * im;
         }
         e += 0.5 * (double)a.modes[m].w * s;
@@ -276,7 +295,7 @@ __device__ void spectral_finalize(const FastArgs& a) {
         const int m = t % a.nm;
         const double k = coef * a.invN * (double)a.modes[m].w;
         double* p = a.acc + 2 * t;
-        a.fh_next[t] = make_float2((float)(k * __ldcg(p)), (float)(k * __ldcg(p + 1)));
+        a.fh_next[t] = make_float2((float)(k * p[0]), (float)(k * p[1]));
         p[0] = 0.0;
         p[1] = 0.0;
     }
@@ -394,7 +413,7 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
     // record-site values read from HBM one plane ahead (p, and u without LES)
     float pf_dp[2], pf_u[2][3];
     auto prefetch = [&](int zr) {
-        const unsigned zo = (unsigned)pmod(zr, nz) * nxy;
+        const unsigned zo = (unsigned)wrap_near(zr, nz) * nxy;
 #pragma unroll
         for (int j = 0; j < 2; ++j) {
             const bool has = j == 0 || tid < 2 * TX + 2 * EY1;
@@ -411,7 +430,7 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
 
     auto stage = [&](int zz) {  // asynchronous copy of plane zz (wrapped) into its slot
         const int slot = (zz + NSLOT) % NSLOT;
-        const unsigned zo = (unsigned)pmod(zz, nz) * nxy;
+        const unsigned zo = (unsigned)wrap_near(zz, nz) * nxy;
 #pragma unroll
         for (int j = 0; j < 2; ++j) {
             const int k = tid + j * NT;
@@ -432,7 +451,7 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
     // this kx of w f_hat e^{i (ky y + kz z)}
     auto ctable = [&](int zr) {
         float2* C = s_C + ((zr + 2) & 1) * (3 * SNK * EY1);
-        const int zw = pmod(zr, nz);
+        const int zw = wrap_near(zr, nz);
         int i1 = zw, i2 = 2 * zw;
         i2 = i2 >= nz ? i2 - nz : i2;
         const float2 ez1 = a.twz[i1], ez2 = a.twz[i2];
@@ -491,7 +510,7 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
             const Rec r = make_record<LES>(a, stc[c2], v, w, u1, u2, u3, pf_dp[j], mn, mx);
             float F[3] = {0.f, 0.f, 0.f};
             if (FMODE == F_ARRAY) {
-                const unsigned s = (unsigned)pmod(zr, nz) * nxy + roff[j];
+                const unsigned s = (unsigned)wrap_near(zr, nz) * nxy + roff[j];
                 F[0] = __ldg(a.force + s);
                 F[1] = __ldg(a.force + N + s);
                 F[2] = __ldg(a.force + 2 * N + s);
@@ -515,6 +534,10 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
     };
 
     // ---- prologue: records of planes z0-1, z0, z0+1 ----
+    // Records of plane zr need the staged planes zr-1..zr+1; the chunk needs
+    // records z0-1..z1, so planes z0-2..z1+1 are staged. Plane zz is staged
+    // right after the barrier that retires the last reader of its slot, half an
+    // iteration before its first use.
     stage(z0 - 2);
     stage(z0 - 1);
     stage(z0);
@@ -536,18 +559,18 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
     if (SPEC) ctable(z0 + 1);
     cp_async_wait_all();
     __syncthreads();
+    if (z0 + 3 <= z1 + 1) stage(z0 + 3);  // slot of z0-1, last read by records(z0)
     records(z0 + 1);
-    prefetch(z0 + 2);
+    if (z0 + 2 <= z1) prefetch(z0 + 2);
 
     float bmin = INFINITY, bmax = -INFINITY;
     bool bad = false;
 
     for (int z = z0; z < z1; ++z) {
-        stage(z + 3);
         // populations of the destination plane, pulled from x - c_i
         unsigned zo[3];
 #pragma unroll
-        for (int d = 0; d < 3; ++d) zo[d] = (unsigned)pmod(z - 1 + d, nz) * nxy;
+        for (int d = 0; d < 3; ++d) zo[d] = (unsigned)wrap_near(z - 1 + d, nz) * nxy;
         float fin[Q], gin[Q];
         if (act) {
 #pragma unroll
@@ -557,11 +580,12 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
                 gin[i] = Pop<ST>::ld(a.g, (unsigned)i * N + src);
             }
         }
-        if (SPEC) ctable(z + 2);
-        cp_async_wait_all();
+        if (SPEC && z + 2 <= z1) ctable(z + 2);
+        cp_async_wait_all();  // plane z+3
         __syncthreads();
-        records(z + 2);
-        prefetch(z + 3);
+        if (z + 4 <= z1 + 1) stage(z + 4);  // slot of plane z, last read by records(z+1)
+        if (z + 2 <= z1) records(z + 2);
+        if (z + 3 <= z1) prefetch(z + 3);
         if (act) {
             float fo[Q], go[Q];
 #pragma unroll
@@ -719,11 +743,10 @@ __device__ void project_rows(const FastArgs& a, long long row0, long long row1, 
             const int m = lane + 32 * j;
             if (m >= a.nm) continue;
             const int4 md = __ldg(a.modes + m);
-            int iy = md.y * y;
+            // (k y) mod n for |k| <= SK: k y lies in (-SK n, SK n)
+            int iy = (md.y * y) % ny;
             iy = iy < 0 ? iy + ny : iy;
-            iy = iy >= ny ? iy - ny : iy;
-            int iz = md.z * z;
-            iz = iz >= nz ? iz - nz : iz;
+            const int iz = (md.z * z) % nz;
             const float2 ey = a.twy[iy], ez = a.twz[iz];
             const float pr = ey.x * ez.x - ey.y * ez.y;
             const float pi = -(ey.x * ez.y + ey.y * ez.x);
@@ -759,7 +782,7 @@ __device__ void project_rows(const FastArgs& a, long long row0, long long row1, 
         const int part = t & 1, cm = t >> 1, c = cm / a.nm, m = cm % a.nm;
         float s = 0.f;
         for (int w = 0; w < PROJ_NT / 32; ++w) s += red[w][c][m][part];
-        atomicAdd(a.acc + 2 * (c * a.nm + m) + part, (double)s);
+        atomicAdd(a.acc + (size_t)(blockIdx.x % SP_NREP) * (6 * a.nm) + 2 * (c * a.nm + m) + part, (double)s);
     }
     __threadfence();
     __shared__ int s_last;
@@ -1040,8 +1063,8 @@ static int fast_spectral_alloc(dl_handle* h) {
         DL_CUDA(h, cudaMalloc(&fs.d_fh[k], sizeof(float2) * 3 * fs.nm));
         DL_CUDA(h, cudaMemset(fs.d_fh[k], 0, sizeof(float2) * 3 * fs.nm));
     }
-    DL_CUDA(h, cudaMalloc(&fs.d_acc, sizeof(double) * 2 * 3 * fs.nm));
-    DL_CUDA(h, cudaMemset(fs.d_acc, 0, sizeof(double) * 2 * 3 * fs.nm));
+    DL_CUDA(h, cudaMalloc(&fs.d_acc, sizeof(double) * 2 * 3 * fs.nm * SP_NREP));
+    DL_CUDA(h, cudaMemset(fs.d_acc, 0, sizeof(double) * 2 * 3 * fs.nm * SP_NREP));
     fs.dirty = 1;
     return DL_OK;
 }
@@ -1157,7 +1180,7 @@ static int fast_spectral_project(dl_handle* h) {
     FastSpectral& fs = h->fsp;
     DL_LAUNCH(h, false, (sp_fhat_from_uh<<<1, 256, 0, h->stream>>>(h->sp.d_uh, h->sp.K, fs.d_modes, fs.nm,
                                                                   0.5 * h->P.eps, fs.d_fh[fs.par], h->d_state)));
-    DL_CUDA(h, cudaMemsetAsync(fs.d_acc, 0, sizeof(double) * 2 * 3 * fs.nm, h->stream));
+    DL_CUDA(h, cudaMemsetAsync(fs.d_acc, 0, sizeof(double) * 2 * 3 * fs.nm * SP_NREP, h->stream));
     DL_CUDA(h, cudaGetLastError());
     fs.dirty = 0;
     return DL_OK;
