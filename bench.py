@@ -30,7 +30,11 @@ sys.path.insert(0, ROOT)
 METRIC = "MLUPS and % HBM roofline, chosen vs plain FP64 form at stated φ error; adjoint/fwd"
 UNIT = "MLUPS"
 # algorithmic bytes per lattice update: 2 distributions x 15 x (read + write) x bytes per population
-BYTES_PER_SITE = {64: 480, 32: 240, 16: 120}
+BYTES_PER_SITE = {64: 480, 32: 240, 16: 120}  # two distributions; the single-phase step moves half
+
+
+def bytes_per_site(form: int, single: bool) -> int:
+    return BYTES_PER_SITE[form] // (2 if single else 1)
 FORMS = {"fp64": 64, "fp32": 32, "fp16": 16}
 DTYPE = {64: "f64", 32: "f32", 16: "f32 (f16 storage)"}
 MAIN_KERNEL = {64: "collide_fp64", 32: "step_fused", 16: "step_fused"}
@@ -126,6 +130,8 @@ def make_workload(name: str, form: int):
     elif name == "config3":
         w = configs.config3()
         w.form = form
+    elif name == "precursor":
+        w = configs.precursor(form=form)
     else:
         raise SystemExit(f"unknown workload {name}")
     return w
@@ -134,7 +140,7 @@ def make_workload(name: str, form: int):
 def new_sim(w, rank: int = 0):
     from droplet_gb300.solver import Droplet
 
-    sim = Droplet(w.params, w.shape, w.form)
+    sim = Droplet(w.params, w.shape, w.form, single_phase=w.single_phase)
     sim.set_fields(**w.fields)
     sim.init_equilibrium()
     sim.set_force(w.force_mode)
@@ -149,7 +155,7 @@ def cpu_baseline(w, budget_s: float = 15.0, threads: int | None = None):
     threads = threads or os.cpu_count() or 1
     pyoracle.set_threads(threads)
     nx, ny, nz = w.shape
-    o = pyoracle.OracleDroplet(w.params, w.shape)
+    o = pyoracle.OracleDroplet(w.params, w.shape, single_phase=w.single_phase)
     o.set_fields(**w.fields)
     o.init_equilibrium()
     o.set_force(w.force_mode)
@@ -183,7 +189,7 @@ def run_reference(args):
     pyoracle.set_threads(threads)
     nx, ny, nz = w.shape
     # probe the per-site rate on one step of the full domain
-    o = pyoracle.OracleDroplet(w.params, w.shape)
+    o = pyoracle.OracleDroplet(w.params, w.shape, single_phase=w.single_phase)
     o.set_fields(**w.fields)
     o.init_equilibrium()
     o.set_force(w.force_mode)
@@ -196,7 +202,7 @@ def run_reference(args):
     nz_s = int(max(8, min(nz, budget * rate / (nx * ny * max(total_steps, 1)))))
     sub = dict((k, np.ascontiguousarray(v[:nz_s])) for k, v in w.fields.items())
     P = w.params
-    o = pyoracle.OracleDroplet(P, (nx, ny, nz_s))
+    o = pyoracle.OracleDroplet(P, (nx, ny, nz_s), single_phase=w.single_phase)
     o.set_fields(**sub)
     o.init_equilibrium()
     o.set_force(w.force_mode)
@@ -281,9 +287,9 @@ def run_ours(args):
     # roofline of the dominant kernel (live per-launch events over the timed region)
     peak, peak_kind = measured_peak_gbs()
     avg_main_ms = prof["main_ms"] / max(prof["main_launches"], 1)
-    bytes_per_launch = BYTES_PER_SITE[form] * N
+    bytes_per_launch = bytes_per_site(form, w.single_phase) * N
     achieved = bytes_per_launch / (avg_main_ms / 1e3) / 1e9
-    traffic = committed_traffic(MAIN_KERNEL[form], w.name)
+    traffic = committed_traffic(f"{MAIN_KERNEL[form]}_{args.form}", w.name)
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_kind,
                 "kernel": MAIN_KERNEL[form], "kernel_ms": round(avg_main_ms, 5),
@@ -298,10 +304,11 @@ def run_ours(args):
         out = {k: torch.empty(v.shape, dtype=torch.float64).pin_memory().numpy() for k, v in w.fields.items()}
         from droplet_gb300.solver import Droplet
 
-        sim2 = Droplet(w.params, w.shape, w.form)
+        sim2 = Droplet(w.params, w.shape, w.form, single_phase=w.single_phase)
         sim2.set_stream(stream.cuda_stream)
         if tune is not None:
             sim2.set_option("lz", tune["lz"])
+            sim2.set_option("prefetch", tune["prefetch"])
         torch.cuda.synchronize()
         if dist is not None:
             dist.barrier()
@@ -348,7 +355,7 @@ def run_ours(args):
             "config": {"workload": w.name, "form": args.form, "sites": N, "shape": list(w.shape),
                        "seed": w.seed, "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                        "l2": "inputs larger than L2 (populations {:.0f} MB)".format(
-                           2 * 15 * N * BYTES_PER_SITE[form] / 60 / 1e6),
+                           bytes_per_site(form, w.single_phase) * N / 2 / 1e6),
                        "notes": w.notes,
                        "tune": None if tune is None else {k: v for k, v in tune.items() if k != "timings"}},
             "roofline": roofline,

@@ -30,6 +30,7 @@ STATUS_TEXT = {
 DL_FORM_FP64 = 64
 DL_FORM_FP32 = 32
 DL_FORM_FP16 = 16
+DL_SINGLE_PHASE = 0x100
 
 DL_FORCE_NONE = 0
 DL_FORCE_STATIC = 1

@@ -71,26 +71,32 @@ def _key(kind: str, form: int, shapes, extra: str) -> str:
 
 
 def tune_droplet(sim, steps: int = 20, use_cache: bool = True) -> dict:
-    """Pick "lz" for one Droplet (fast forms). Returns the chosen settings."""
+    """Pick "lz" and "prefetch" for one Droplet (fast forms). Returns the
+    chosen settings."""
     p = sim.params
-    key = _key("single", sim.form, [(sim.nx, sim.ny, sim.nz)], f"les{int(bool(p.les))}")
+    key = _key("single", sim.form, [(sim.nx, sim.ny, sim.nz)],
+               f"les{int(bool(p.les))}" + ("_1phase" if getattr(sim, "single_phase", False) else "") + "_pf")
     if use_cache:
         hit = _load().get(key)
         if hit:
             sim.set_option("lz", hit["lz"])
+            sim.set_option("prefetch", hit["prefetch"])
             return dict(hit, cached=True)
     best = None
     timings = {}
-    for lz in LZ_CANDIDATES:
-        if lz > sim.nz:
-            continue
-        sim.set_option("lz", lz)
-        ms = _time_steps(sim, steps)
-        timings[str(lz)] = ms
-        if best is None or ms < best[1]:
-            best = (lz, ms)
+    for pf in (0, 1):
+        sim.set_option("prefetch", pf)
+        for lz in LZ_CANDIDATES:
+            if lz > sim.nz:
+                continue
+            sim.set_option("lz", lz)
+            ms = _time_steps(sim, steps)
+            timings[f"lz{lz}_pf{pf}"] = ms
+            if best is None or ms < best[2]:
+                best = (lz, pf, ms)
     sim.set_option("lz", best[0])
-    res = {"lz": best[0], "ms_per_step": best[1], "timings": timings}
+    sim.set_option("prefetch", best[1])
+    res = {"lz": best[0], "prefetch": best[1], "ms_per_step": best[2], "timings": timings}
     _store(key, res)
     return dict(res, cached=False)
 

@@ -39,6 +39,7 @@ class Workload:
     force_mode: int
     seed: int
     notes: str = ""
+    single_phase: bool = False  # the g-only precursor step (DL_SINGLE_PHASE)
 
     @property
     def n_sites(self) -> int:
@@ -161,4 +162,27 @@ def config5(n: int = 96) -> Workload:
     return shear_droplet(n=n, radius=18.0 * n / 96.0, U=0.04, form=_abi.DL_FORM_FP32, steps=500)
 
 
-WORKLOADS = {"config1": config1, "config2": config2, "config3": config3, "config4": config4, "config5": config5}
+def precursor(n: int = 256, form: int = _abi.DL_FORM_FP32, steps: int = 2000, nu: float = 0.001, kc: int = 3,
+              eta: float = 1.0) -> Workload:
+    """Single-phase forced turbulence, the precursor program
+    program/lbm_iht_xy.f90: nu = 0.001, band forcing on 1 <= |k| < kc = 3 with
+    eps = nu^3 / eta^4 (Kolmogorov scale eta = 1 ds, :31-34), started from its
+    Taylor-Green-like field (ini, :238-243): u1 = -A cos(kx) sin(kz),
+    u3 = A sin(kx) cos(kz), p = 1/3 - A^2/4 (cos 2kx + cos 2kz), A = 1e-4."""
+    shape = (n, n, n)
+    eps = nu ** 3 / eta ** 4
+    P = Params.lbm_drop_xy().replace(nu1=nu, nu2=nu, kappaf=0.0, kappag=0.0, eps=eps, kc=kc,
+                                     visc_mode=_abi.DL_VISC_FIXED)
+    x, y, z = init_fields.grid(shape)
+    k = 2.0 * np.pi / n
+    A = 1e-4
+    u1 = -A * np.cos(k * x) * np.sin(k * z)
+    u3 = A * np.sin(k * x) * np.cos(k * z)
+    p = 1.0 / 3.0 - A * A / 4.0 * (np.cos(2.0 * k * x) + np.cos(2.0 * k * z))
+    f = init_fields.fields(np.full(shape[::-1], P.phi1), u1, np.zeros_like(u1), u3, p)
+    return Workload(f"precursor_turbulence_{n}^3", P, shape, form, steps, f, _abi.DL_FORCE_SPECTRAL, 0,
+                    f"single phase, nu={nu} eps={eps:.3g} kc={kc}", single_phase=True)
+
+
+WORKLOADS = {"config1": config1, "config2": config2, "config3": config3, "config4": config4, "config5": config5,
+             "precursor": precursor}

@@ -263,7 +263,8 @@ static void fill_adj(dl_handle* h, AdjArgs& a) {
 }
 
 int adjoint_check(dl_handle* h) {
-    if (h->form != DL_FORM_FP32) return set_error(h, DL_ERR_UNSUPPORTED, "the adjoint is implemented for the FP32 form");
+    if (h->form != DL_FORM_FP32 || h->single)
+        return set_error(h, DL_ERR_UNSUPPORTED, "the adjoint is implemented for the two-phase FP32 form");
     if (h->P.les) return set_error(h, DL_ERR_UNSUPPORTED, "the adjoint does not cover the Smagorinsky term");
     if (h->P.nu2 != h->P.nu1) return set_error(h, DL_ERR_UNSUPPORTED, "the adjoint assumes viscosity ratio 1");
     if (h->force_mode == DL_FORCE_SPECTRAL) return set_error(h, DL_ERR_UNSUPPORTED, "the adjoint covers no spectral force");

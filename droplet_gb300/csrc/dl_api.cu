@@ -140,7 +140,10 @@ int dl_create(const dl_params* params, int nx, int ny, int nz, int form, dl_hand
     if (!params || !out) return DL_ERR_ARG;
     *out = nullptr;
     if (nx < 3 || ny < 3 || nz < 3) return DL_ERR_ARG;
+    const bool single = (form & DL_SINGLE_PHASE) != 0;
+    form &= ~DL_SINGLE_PHASE;
     if (form != DL_FORM_FP64 && form != DL_FORM_FP32 && form != DL_FORM_FP16) return DL_ERR_UNSUPPORTED;
+    if (single && (params->les != 0 || params->Anu != 0.0)) return DL_ERR_UNSUPPORTED;
     if (params->tauf <= 0.5 || params->ds <= 0.0 || params->phi2 == params->phi1) return DL_ERR_ARG;
     if (params->kc < 0 || params->visc_mode < 0 || params->visc_mode > 1) return DL_ERR_ARG;
     dl_handle* h = new (std::nothrow) dl_handle();
@@ -152,6 +155,17 @@ int dl_create(const dl_params* params, int nx, int ny, int nz, int form, dl_hand
     h->nz = nz;
     h->N = (size_t)nx * ny * nz;
     h->form = form;
+    h->single = single;
+    // L2 prefetch of the next plane's pulled rows: pays off where arithmetic,
+    // not bandwidth, sets the pace (the two-phase FP32 step); "prefetch" option
+    h->l2_prefetch = (!single && form == DL_FORM_FP32) ? 1 : 0;
+    if (single) {
+        // the precursor step: constant nu1, no interface terms
+        h->P.kappaf = 0.0;
+        h->P.kappag = 0.0;
+        h->P.nu2 = h->P.nu1;
+        h->P.visc_mode = DL_VISC_FIXED;
+    }
     h->stream = 0;
     h->force_mode = DL_FORCE_NONE;
     cudaError_t e = cudaGetDevice(&h->device);
@@ -221,6 +235,7 @@ int dl_profile_read(dl_handle* h, dl_profile_stats* out) {
 int dl_label_droplets(dl_handle* h, int connectivity, int32_t* labels, int64_t* ndrops, double* volumes,
                       int64_t max_volumes) {
     if (!h || !ndrops || (max_volumes > 0 && !volumes) || max_volumes < 0) return DL_ERR_ARG;
+    if (h->single) return set_error(h, DL_ERR_UNSUPPORTED, "no droplets in the single-phase step");
     long long n = 0;
     int rc = label_droplets(h, connectivity, (int*)labels, &n, volumes, (long long)max_volumes);
     *ndrops = (int64_t)n;
@@ -229,14 +244,16 @@ int dl_label_droplets(dl_handle* h, int connectivity, int32_t* labels, int64_t* 
 
 int dl_state_floats(dl_handle* h, int64_t* n) {
     if (!h || !n) return DL_ERR_ARG;
-    if (h->form != DL_FORM_FP32) return set_error(h, DL_ERR_UNSUPPORTED, "device state export is for the FP32 form");
+    if (h->form != DL_FORM_FP32 || h->single)
+        return set_error(h, DL_ERR_UNSUPPORTED, "device state export is for the two-phase FP32 form");
     *n = (int64_t)35 * (int64_t)h->N;
     return DL_OK;
 }
 
 int dl_save_state(dl_handle* h, void* d_dst) {
     if (!h || !d_dst) return DL_ERR_ARG;
-    if (h->form != DL_FORM_FP32) return set_error(h, DL_ERR_UNSUPPORTED, "device state export is for the FP32 form");
+    if (h->form != DL_FORM_FP32 || h->single)
+        return set_error(h, DL_ERR_UNSUPPORTED, "device state export is for the two-phase FP32 form");
     const size_t N = h->N;
     float* d = (float*)d_dst;
     DL_CUDA(h, cudaMemcpyAsync(d, h->fs[h->cur], sizeof(float) * Q * N, cudaMemcpyDeviceToDevice, h->stream));
@@ -248,7 +265,8 @@ int dl_save_state(dl_handle* h, void* d_dst) {
 
 int dl_load_state(dl_handle* h, const void* d_src) {
     if (!h || !d_src) return DL_ERR_ARG;
-    if (h->form != DL_FORM_FP32) return set_error(h, DL_ERR_UNSUPPORTED, "device state import is for the FP32 form");
+    if (h->form != DL_FORM_FP32 || h->single)
+        return set_error(h, DL_ERR_UNSUPPORTED, "device state import is for the two-phase FP32 form");
     const size_t N = h->N;
     const float* d = (const float*)d_src;
     DL_CUDA(h, cudaMemcpyAsync(h->fs[h->cur], d, sizeof(float) * Q * N, cudaMemcpyDeviceToDevice, h->stream));
@@ -287,6 +305,11 @@ int dl_set_option(dl_handle* h, const char* key, int64_t value) {
         h->lz = value == 0 ? 16 : (int)value;
         return DL_OK;
     }
+    if (strcmp(key, "prefetch") == 0) {
+        if (value < 0 || value > 1) return set_error(h, DL_ERR_ARG, "prefetch must be 0 or 1");
+        h->l2_prefetch = (int)value;
+        return DL_OK;
+    }
     return set_error(h, DL_ERR_ARG, "unknown option '%s'", key);
 }
 
@@ -294,6 +317,10 @@ int dl_get_option(dl_handle* h, const char* key, int64_t* value) {
     if (!h || !key || !value) return DL_ERR_ARG;
     if (strcmp(key, "lz") == 0) {
         *value = h->lz;
+        return DL_OK;
+    }
+    if (strcmp(key, "prefetch") == 0) {
+        *value = h->l2_prefetch;
         return DL_OK;
     }
     return set_error(h, DL_ERR_ARG, "unknown option '%s'", key);
@@ -316,8 +343,14 @@ int dl_set_fields(dl_handle* h, const double* phi, const double* u1, const doubl
         d = st.d;
     }
     const double* src[5] = {phi, u1, u2, u3, p};
-    for (int k = 0; k < 5; ++k)
+    for (int k = 0; k < 5; ++k) {
+        if (k == 0 && h->single) {  // single phase: phi is not a field
+            int rc = fill_doubles(h, d, h->P.phi1, N);
+            if (rc != DL_OK) return rc;
+            continue;
+        }
         DL_CUDA(h, cudaMemcpyAsync(d + k * N, src[k], N * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    }
     if (is_fast(h)) {
         int rc = fast_set_fields(h, d);
         if (rc != DL_OK) return rc;
@@ -421,10 +454,15 @@ int dl_get_populations(dl_handle* h, double* f, double* g) {
         return DL_OK;
     }
     DL_CUDA(h, cudaMalloc(&st.d, bytes));
-    int rc = soa_to_aos(h, h->f64[h->cur], st.d);
-    if (rc != DL_OK) return rc;
-    DL_CUDA(h, cudaMemcpyAsync(f, st.d, bytes, cudaMemcpyDeviceToHost, h->stream));
-    DL_CUDA(h, cudaStreamSynchronize(h->stream));
+    int rc = DL_OK;
+    if (h->single) {
+        memset(f, 0, bytes);  // single phase: no f
+    } else {
+        rc = soa_to_aos(h, h->f64[h->cur], st.d);
+        if (rc != DL_OK) return rc;
+        DL_CUDA(h, cudaMemcpyAsync(f, st.d, bytes, cudaMemcpyDeviceToHost, h->stream));
+        DL_CUDA(h, cudaStreamSynchronize(h->stream));
+    }
     rc = soa_to_aos(h, h->g64[h->cur], st.d);
     if (rc != DL_OK) return rc;
     DL_CUDA(h, cudaMemcpyAsync(g, st.d, bytes, cudaMemcpyDeviceToHost, h->stream));
@@ -448,10 +486,13 @@ int dl_set_populations(dl_handle* h, const double* f, const double* g) {
         return DL_OK;
     }
     DL_CUDA(h, cudaMalloc(&st.d, bytes));
-    DL_CUDA(h, cudaMemcpyAsync(st.d, f, bytes, cudaMemcpyHostToDevice, h->stream));
-    int rc = aos_to_soa(h, st.d, h->f64[h->cur]);
-    if (rc != DL_OK) return rc;
-    DL_CUDA(h, cudaStreamSynchronize(h->stream));
+    int rc = DL_OK;
+    if (!h->single) {  // single phase: f is ignored
+        DL_CUDA(h, cudaMemcpyAsync(st.d, f, bytes, cudaMemcpyHostToDevice, h->stream));
+        rc = aos_to_soa(h, st.d, h->f64[h->cur]);
+        if (rc != DL_OK) return rc;
+        DL_CUDA(h, cudaStreamSynchronize(h->stream));
+    }
     DL_CUDA(h, cudaMemcpyAsync(st.d, g, bytes, cudaMemcpyHostToDevice, h->stream));
     rc = aos_to_soa(h, st.d, h->g64[h->cur]);
     if (rc != DL_OK) return rc;

@@ -116,6 +116,7 @@ struct dl_handle {
     int force_mode;
     bool fields_set;
     bool eq_init;
+    bool single;             // single-phase step (g only, DL_SINGLE_PHASE)
     char err[512];
 
     dl::LatticeConsts lc;
@@ -135,6 +136,7 @@ struct dl_handle {
     float* mac32[2];         // [5][N]: phi - phi1, u1, u2, u3, p - 1/3
     float* force32;          // [3][N]
     int lz;                  // z planes per block of the fused kernel
+    int l2_prefetch;         // fused kernel: bulk L2 prefetch of the next plane's pulls
 
     dl::SpectralPlan sp;
     dl::FastSpectral fsp;
@@ -203,6 +205,7 @@ int adjoint_grads(dl_handle* h, double* out4);
 // transposes (layout.cu)
 int soa_to_aos(dl_handle* h, const double* d_soa, double* d_aos);
 int aos_to_soa(dl_handle* h, const double* d_aos, double* d_soa);
+int fill_doubles(dl_handle* h, double* d, double v, size_t n);
 // diagnostics (reduce.cu)
 int reduce_fields(dl_handle* h, const double* d_mac, dl_diag* out);
 int reduce_fields_f32(dl_handle* h, const float* d_mac, dl_diag* out);

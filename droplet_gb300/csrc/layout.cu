@@ -37,4 +37,16 @@ int aos_to_soa(dl_handle* h, const double* d_aos, double* d_soa) {
     return DL_OK;
 }
 
+__global__ void fill_kernel(double* __restrict__ d, double v, long long n) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t < n) d[t] = v;
+}
+
+int fill_doubles(dl_handle* h, double* d, double v, size_t n) {
+    if (n == 0) return DL_OK;
+    DL_LAUNCH(h, false, fill_kernel<<<(unsigned)((n + 255) / 256), 256, 0, h->stream>>>(d, v, (long long)n));
+    DL_CUDA(h, cudaGetLastError());
+    return DL_OK;
+}
+
 }  // namespace dl

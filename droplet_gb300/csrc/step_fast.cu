@@ -62,6 +62,7 @@ constexpr int SP_NREP = 16;           // copies of the projection accumulators (
 
 struct FastArgs {
     int nx, ny, nz, lz;
+    int l2_prefetch;
     long long N;
     const float* mac;  // [5][N] dphi, u1, u2, u3, dp
     float* maco;
@@ -72,6 +73,7 @@ struct FastArgs {
     const float* force;  // [3][N] (F_ARRAY)
     DevState* st;
     float phi1, phi2, omf, kf, kf6, kg, T, a, b, omb1, nu1, dnu, csd, anu23, inv_ds, inv_lap, inv_grad;
+    float omg_sp;  // 1/tau_g of the single-phase step, tau_g = 1/2 + 3 nu1/ds
     float fref[Q];   // bulk equilibrium of f (FP32 form offsets)
     float wall_bot[5], wall_top[5];
     int walls, visc_fixed;
@@ -181,6 +183,7 @@ struct Pop<__half> {
 // ---- the per-site record ------------------------------------------------------
 struct Rec {
     float dphi, u1, u2, u3, dA, S, omg, gx, gy, gz, gsq, dp0, Fx, Fy, Fz;
+    float gq;  // 1.5 |grad phi|^2 (stored records of the FP32 form)
 };
 
 // v[1..14]: dphi at the D3Q15 neighbours; w[c][1..14]: u_c there (LES only)
@@ -233,7 +236,7 @@ __device__ __forceinline__ void collide_dir(const FastArgs& a, int i, const Rec&
     const float phi = __fadd_rn(a.phi1, r.dphi);
     const float cu = (i == 0) ? 0.f : cdot3(i, r.u1, r.u2, r.u3);
     const float cg = (i == 0) ? 0.f : cdot3(i, r.gx, r.gy, r.gz);
-    const float cGc = 4.5f * cg * cg - 1.5f * c2w(i) * r.gsq;
+    const float cGc = RES ? 4.5f * cg * cg - 1.5f * c2w(i) * r.gsq : (4.5f * cg) * cg - c2w(i) * r.gq;
     const float E = Ew(i);
     if (!RES) {
         const float dfeq = (i == 0 ? r.dphi : 0.f) + Fw(i) * r.dA + E * (3.f * phi * cu + a.kf * cGc);
@@ -248,6 +251,24 @@ __device__ __forceinline__ void collide_dir(const FastArgs& a, int i, const Rec&
         go = gb + gin + r.omg * (E * a.kg * cGc - gin);
     }
     if (FORCE && i != 0) go += 3.f * E * cdot3(i, r.Fx, r.Fy, r.Fz);
+}
+
+// single-phase collision of g_i at its source (g_cal, program/lbm_iht_xy.f90:561-590):
+// the two-phase rule without the interface terms
+template <bool RES, bool FORCE>
+__device__ __forceinline__ float collide_g(int i, float S, float omg, float u1, float u2, float u3, float Fx,
+                                           float Fy, float Fz, float gin) {
+    const float cu = (i == 0) ? 0.f : cdot3(i, u1, u2, u3);
+    const float E = Ew(i);
+    float go;
+    if (!RES) {
+        const float dgeq = E * (S + cu * (3.f + 4.5f * cu));
+        go = gin + omg * (dgeq - gin);
+    } else {
+        go = gbar(i, S, cu) + gin + omg * (0.f - gin);
+    }
+    if (FORCE && i != 0) go += 3.f * E * cdot3(i, Fx, Fy, Fz);
+    return go;
 }
 
 // last block: band energy E = sum_m 0.5 w_m |u_hat_m|^2, u_hat = acc / N, and
@@ -305,7 +326,7 @@ __device__ void spectral_finalize(const FastArgs& a) {
 // Per z plane one barrier: the staging ring and the record ring have four
 // slots; the records of plane z+2 are built in the same barrier interval as
 // the pull of plane z. Records are float4 groups:
-//   q0 = (dphi, u1, u2, u3), q1 = (gx, gy, gz, dA), q2 = (S, 1/tau_g, dp0, Fx),
+//   q0 = (dphi, u1, u2, u3), q1 = (gx, gy, gz, dA), q2 = (S, 1/tau_g, dp0 (FP16) or 1.5|grad phi|^2 (FP32), Fx),
 //   q3 = (Fy, Fz) (with a force only).
 constexpr int NSLOT = 4;
 
@@ -314,12 +335,16 @@ __device__ __forceinline__ void cp_async4(float* smem_dst, const float* gmem_src
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem_src) : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+// bulk prefetch of [p, p + bytes) into L2 (16-byte aligned, bytes a multiple of 16)
+__device__ __forceinline__ void prefetch_l2(const void* p, unsigned bytes) {
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;\n" ::"l"(p), "r"(bytes) : "memory");
+}
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
 // shared-memory footprint (floats) of the fused kernel
 __host__ __device__ constexpr int fused_smem_floats(bool les, bool spec, bool force) {
     return NSLOT * P2 * (les ? 4 : 1) + NSLOT * P1 * (12 + (force ? 2 : 0)) +
-           (spec ? 2 * (2 * 3 * SNK * EY1) + 2 * (SNK * EX1 + SNK * EY1) : 0);
+           (spec ? 2 * (2 * 3 * SNK * EY1) + 2 * (SNK * EX1 + SNK * EY1) + 2 * (3 * 3 * SNK * EY1) : 0);
 }
 
 // the thread's (at most two) record positions: pass A = its own column
@@ -350,7 +375,8 @@ __device__ __forceinline__ RecPos rec_pos(int tid, int j) {
     return r;
 }
 
-template <typename ST, bool RES, bool LES, int FMODE>
+// SP: the single-phase step (g only; no staging, no phi stencils)
+template <typename ST, bool RES, bool LES, int FMODE, bool SP = false>
 __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int bx, int by, int bz, unsigned nblk) {
     constexpr bool FORCE = FMODE != F_NONE;
     constexpr bool SPEC = FMODE == F_SPECTRAL;
@@ -363,6 +389,7 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
     float2* s_C = s_q3 + (FORCE ? NSLOT * P1 : 0);       // [2][3][SNK][EY1] (SPEC)
     float2* s_tx = s_C + 2 * 3 * SNK * EY1;              // [SNK][EX1] e^{i kx x}
     float2* s_ty = s_tx + SNK * EX1;                     // [SNK][EY1] e^{i ky y}
+    float2* s_D = s_ty + SNK * EY1;                      // [3][SNK][EY1][3] z-free part of C, by kz
     const int tid = threadIdx.x;
     const int tx = tid % TX, ty = tid / TX;
     const int nx = a.nx, ny = a.ny, nz = a.nz;
@@ -429,6 +456,7 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
     };
 
     auto stage = [&](int zz) {  // asynchronous copy of plane zz (wrapped) into its slot
+        if constexpr (SP) return;
         const int slot = (zz + NSLOT) % NSLOT;
         const unsigned zo = (unsigned)wrap_near(zz, nz) * nxy;
 #pragma unroll
@@ -448,28 +476,40 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
     };
 
     // force synthesis table of plane zr: C[c][kx][row] = sum over the modes with
-    // this kx of w f_hat e^{i (ky y + kz z)}
-    auto ctable = [&](int zr) {
-        float2* C = s_C + ((zr + 2) & 1) * (3 * SNK * EY1);
-        const int zw = wrap_near(zr, nz);
-        int i1 = zw, i2 = 2 * zw;
-        i2 = i2 >= nz ? i2 - nz : i2;
-        const float2 ez1 = a.twz[i1], ez2 = a.twz[i2];
-        for (int t = tid; t < 3 * SNK * EY1; t += NT) {
-            const int yy = t % EY1, r = t / EY1, kxi = r % SNK, c = r / SNK;
+    // this kx of w f_hat e^{i (ky y + kz z)} = sum_kz D[c][kx][row][kz] e^{i kz z},
+    // D built once per block (dtable), C per plane from the two z twiddles
+    auto dtable = [&]() {
+        for (int t = tid; t < 3 * SNK * EY1 * 3; t += NT) {
+            const int kz = t % 3, r = t / 3, yy = r % EY1, r2 = r / EY1, kxi = r2 % SNK, c = r2 / SNK;
             float re = 0.f, im = 0.f;
             const int m1 = a.kx_off[kxi + 1];
             for (int m = a.kx_off[kxi]; m < m1; ++m) {
                 const int4 md = __ldg(a.modes + m);
+                if (md.z != kz) continue;
                 const float2 ey = s_ty[(md.y + SK) * EY1 + yy];
-                const float2 ez = md.z == 0 ? make_float2(1.f, 0.f) : (md.z == 1 ? ez1 : ez2);
-                const float pr = ey.x * ez.x - ey.y * ez.y, pi = ey.x * ez.y + ey.y * ez.x;
                 const float2 fv = __ldg(a.fh + c * a.nm + m);
-                re += fv.x * pr - fv.y * pi;
-                im += fv.x * pi + fv.y * pr;
+                re += fv.x * ey.x - fv.y * ey.y;
+                im += fv.x * ey.y + fv.y * ey.x;
             }
-            C[t] = make_float2(re, im);
+            s_D[t] = make_float2(re, im);
         }
+    };
+    auto ctable = [&](int zr, float2 ez1, float2 ez2) {
+        float2* C = s_C + ((zr + 2) & 1) * (3 * SNK * EY1);
+        // the last warps take the table: the first ones carry the halo records
+        for (int t = NT - 1 - tid; t < 3 * SNK * EY1; t += NT) {
+            const float2 d0 = s_D[3 * t], d1 = s_D[3 * t + 1], d2 = s_D[3 * t + 2];
+            C[t] = make_float2(d0.x + (d1.x * ez1.x - d1.y * ez1.y) + (d2.x * ez2.x - d2.y * ez2.y),
+                               d0.y + (d1.x * ez1.y + d1.y * ez1.x) + (d2.x * ez2.y + d2.y * ez2.x));
+        }
+    };
+    // e^{i z} and e^{2 i z} of plane zr
+    auto ztw = [&](int zr, float2& ez1, float2& ez2) {
+        const int zw = wrap_near(zr, nz);
+        int i2 = 2 * zw;
+        i2 = i2 >= nz ? i2 - nz : i2;
+        ez1 = __ldg(a.twz + zw);
+        ez2 = __ldg(a.twz + i2);
     };
 
     auto records = [&](int zr) {
@@ -482,6 +522,31 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
         for (int j = 0; j < 2; ++j) {
             const RecPos rp = rec_pos(tid, j);
             if (!rp.has) continue;
+            float F[3] = {0.f, 0.f, 0.f};
+            if (FMODE == F_ARRAY) {
+                const unsigned s = (unsigned)wrap_near(zr, nz) * nxy + roff[j];
+                F[0] = __ldg(a.force + s);
+                F[1] = __ldg(a.force + N + s);
+                F[2] = __ldg(a.force + 2 * N + s);
+            } else if (SPEC) {
+#pragma unroll
+                for (int kxi = 0; kxi < SNK; ++kxi) {
+                    const float2 e = s_tx[kxi * EX1 + rp.ex];
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        const float2 cv = C[(c * SNK + kxi) * EY1 + rp.ey];
+                        F[c] += cv.x * e.x - cv.y * e.y;
+                    }
+                }
+            }
+            const int o = sc * P1 + rp.k;
+            if constexpr (SP) {
+                const float u1 = pf_u[j][0], u2 = pf_u[j][1], u3 = pf_u[j][2];
+                s_q0[o] = make_float4(0.f, u1, u2, u3);
+                s_q2[o] = make_float4(site_S(pf_dp[j], u1, u2, u3), a.omg_sp, 0.f, F[0]);
+                if (FORCE) s_q3[o] = make_float2(F[1], F[2]);
+                continue;
+            }
             const int c2 = (rp.ey + 1) * EX2 + (rp.ex + 1);
             float v[Q];
 #pragma unroll
@@ -508,28 +573,32 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
                 u3 = pf_u[j][2];
             }
             const Rec r = make_record<LES>(a, stc[c2], v, w, u1, u2, u3, pf_dp[j], mn, mx);
-            float F[3] = {0.f, 0.f, 0.f};
-            if (FMODE == F_ARRAY) {
-                const unsigned s = (unsigned)wrap_near(zr, nz) * nxy + roff[j];
-                F[0] = __ldg(a.force + s);
-                F[1] = __ldg(a.force + N + s);
-                F[2] = __ldg(a.force + 2 * N + s);
-            } else if (SPEC) {
-#pragma unroll
-                for (int kxi = 0; kxi < SNK; ++kxi) {
-                    const float2 e = s_tx[kxi * EX1 + rp.ex];
-#pragma unroll
-                    for (int c = 0; c < 3; ++c) {
-                        const float2 cv = C[(c * SNK + kxi) * EY1 + rp.ey];
-                        F[c] += cv.x * e.x - cv.y * e.y;
-                    }
-                }
-            }
-            const int o = sc * P1 + rp.k;
             s_q0[o] = make_float4(r.dphi, r.u1, r.u2, r.u3);
             s_q1[o] = make_float4(r.gx, r.gy, r.gz, r.dA);
-            s_q2[o] = make_float4(r.S, r.omg, RES ? r.dp0 : 0.f, F[0]);
+            s_q2[o] = make_float4(r.S, r.omg, RES ? r.dp0 : 1.5f * r.gsq, F[0]);
             if (FORCE) s_q3[o] = make_float2(F[1], F[2]);
+        }
+    };
+
+    // L2 prefetch of the rows the pulls of plane zp read: per population array
+    // and direction, the TY source rows y0-c_y.. at plane zp-c_z, columns
+    // x0-1 .. x0+TX (one bulk prefetch per row, clipped to the row and array)
+    auto pull_prefetch = [&](int zp) {
+        constexpr int NARR = SP ? 1 : 2;
+        constexpr unsigned ES = sizeof(ST);
+        const int xa = max(x0 - 1, 0), xb = min(x0 + TX + 1, nx);
+        for (int t = tid; t < NARR * Q * TY; t += NT) {
+            const int r = t % TY, q = t / TY, i = q % Q;
+            const bool isg = SP || q >= Q;
+            const char* base = (const char*)(isg ? a.g : a.f);
+            const size_t arr_end = (size_t)Q * N * ES;
+            const size_t row = (size_t)i * N + (size_t)wrap_near(zp - cz(i), nz) * nxy +
+                               (size_t)nx * (unsigned)wrap_near(y0 + r - cy(i), ny);
+            size_t b0 = (row + (size_t)xa) * ES, b1 = (row + (size_t)xb) * ES;
+            b0 &= ~(size_t)15;
+            b1 = (b1 + 15) & ~(size_t)15;
+            if (b1 > (arr_end & ~(size_t)15)) b1 = arr_end & ~(size_t)15;
+            if (b1 > b0) prefetch_l2(base + b0, (unsigned)(b1 - b0));
         }
     };
 
@@ -545,8 +614,13 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
     prefetch(z0 - 1);
     if (SPEC) {
         __syncthreads();  // s_ty, s_tx
-        ctable(z0 - 1);
-        ctable(z0);
+        dtable();
+        __syncthreads();  // s_D
+        float2 e1, e2;
+        ztw(z0 - 1, e1, e2);
+        ctable(z0 - 1, e1, e2);
+        ztw(z0, e1, e2);
+        ctable(z0, e1, e2);
     }
     cp_async_wait_all();
     __syncthreads();
@@ -556,7 +630,11 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
     prefetch(z0 + 1);
     __syncthreads();
     stage(z0 + 2);
-    if (SPEC) ctable(z0 + 1);
+    if (SPEC) {
+        float2 e1, e2;
+        ztw(z0 + 1, e1, e2);
+        ctable(z0 + 1, e1, e2);
+    }
     cp_async_wait_all();
     __syncthreads();
     if (z0 + 3 <= z1 + 1) stage(z0 + 3);  // slot of z0-1, last read by records(z0)
@@ -567,6 +645,8 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
     bool bad = false;
 
     for (int z = z0; z < z1; ++z) {
+        float2 tz1, tz2;  // twiddles of plane z+2 (their latency hides behind the pulls)
+        if (SPEC) ztw(z + 2, tz1, tz2);
         // populations of the destination plane, pulled from x - c_i
         unsigned zo[3];
 #pragma unroll
@@ -576,14 +656,15 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
 #pragma unroll
             for (int i = 0; i < Q; ++i) {
                 const unsigned src = zo[1 - cz(i)] + yr[1 - cy(i)] + xs[1 - cx(i)];
-                fin[i] = Pop<ST>::ld(a.f, (unsigned)i * N + src);
+                if constexpr (!SP) fin[i] = Pop<ST>::ld(a.f, (unsigned)i * N + src);
                 gin[i] = Pop<ST>::ld(a.g, (unsigned)i * N + src);
             }
         }
-        if (SPEC && z + 2 <= z1) ctable(z + 2);
+        if (SPEC && z + 2 <= z1) ctable(z + 2, tz1, tz2);
         cp_async_wait_all();  // plane z+3
         __syncthreads();
         if (z + 4 <= z1 + 1) stage(z + 4);  // slot of plane z, last read by records(z+1)
+        if (a.l2_prefetch && z + 1 < z1) pull_prefetch(z + 1);
         if (z + 2 <= z1) records(z + 2);
         if (z + 3 <= z1) prefetch(z + 3);
         if (act) {
@@ -591,6 +672,18 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
 #pragma unroll
             for (int i = 0; i < Q; ++i) {
                 const int o = ((z - cz(i) + NSLOT) % NSLOT) * P1 + (ty + 1 - cy(i)) * EX1 + (tx + 1 - cx(i));
+                if constexpr (SP) {
+                    const float4 q0 = s_q0[o], q2 = s_q2[o];
+                    float Fy = 0.f, Fz = 0.f;
+                    if (FORCE) {
+                        const float2 q3 = s_q3[o];
+                        Fy = q3.x;
+                        Fz = q3.y;
+                    }
+                    go[i] = collide_g<RES, FORCE>(i, q2.x, q2.y, q0.y, q0.z, q0.w, q2.w, Fy, Fz, gin[i]);
+                    fo[i] = 0.f;
+                    continue;
+                }
                 const float4 q0 = s_q0[o], q1 = s_q1[o], q2 = s_q2[o];
                 Rec r;
                 r.dphi = q0.x;
@@ -603,8 +696,12 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
                 r.dA = q1.w;
                 r.S = q2.x;
                 r.omg = q2.y;
-                r.dp0 = q2.z;
-                r.gsq = r.gx * r.gx + r.gy * r.gy + r.gz * r.gz;
+                if (RES) {
+                    r.dp0 = q2.z;
+                    r.gsq = r.gx * r.gx + r.gy * r.gy + r.gz * r.gz;
+                } else {
+                    r.gq = q2.z;
+                }
                 if (FORCE) {
                     const float2 q3 = s_q3[o];
                     r.Fx = q2.w;
@@ -636,7 +733,7 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
             float dphin = 0.f, dpn = 0.f, u1n = 0.f, u2n = 0.f, u3n = 0.f;
 #pragma unroll
             for (int i = 0; i < Q; ++i) {
-                dphin += fo[i];
+                if constexpr (!SP) dphin += fo[i];
                 dpn += go[i];
                 if (cx(i) == 1) u1n += go[i];
                 else if (cx(i) == -1) u1n -= go[i];
@@ -654,13 +751,13 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
 #pragma unroll
                 for (int i = 0; i < Q; ++i) {
                     const float cu = (i == 0) ? 0.f : cdot3(i, u1n, u2n, u3n);
-                    Pop<ST>::st(a.fo, (unsigned)i * N + d, fo[i] - fbar(i, dphin, phin, dp0n, cu));
+                    if constexpr (!SP) Pop<ST>::st(a.fo, (unsigned)i * N + d, fo[i] - fbar(i, dphin, phin, dp0n, cu));
                     Pop<ST>::st(a.go, (unsigned)i * N + d, go[i] - gbar(i, Sn, cu));
                 }
             } else {
 #pragma unroll
                 for (int i = 0; i < Q; ++i) {
-                    Pop<ST>::st(a.fo, (unsigned)i * N + d, fo[i]);
+                    if constexpr (!SP) Pop<ST>::st(a.fo, (unsigned)i * N + d, fo[i]);
                     Pop<ST>::st(a.go, (unsigned)i * N + d, go[i]);
                 }
             }
@@ -679,11 +776,11 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
                                      (double)a.phi2, bad, a.step, nblk);
 }
 
-template <typename ST, bool RES, bool LES, int FMODE>
+template <typename ST, bool RES, bool LES, int FMODE, bool SP = false>
 __global__ void __launch_bounds__(NT, 2) step_fused(const FastArgs a) {
     extern __shared__ float smem[];
-    fused_body<ST, RES, LES, FMODE>(a, smem, blockIdx.x, blockIdx.y, blockIdx.z,
-                                    gridDim.x * gridDim.y * gridDim.z);
+    fused_body<ST, RES, LES, FMODE, SP>(a, smem, blockIdx.x, blockIdx.y, blockIdx.z,
+                                        gridDim.x * gridDim.y * gridDim.z);
 }
 
 // ---- band projection of the new u (F_SPECTRAL) ---------------------------------------
@@ -833,10 +930,10 @@ __global__ void __launch_bounds__(256) init_fast(const FastArgs a) {
         const float dfeq = (i == 0 ? r.dphi : 0.f) + Fw(i) * r.dA + E * (3.f * phi * cu + a.kf * cGc);
         const float dgeq = E * (r.S + cu * (3.f + 4.5f * cu) + a.kg * cGc);
         if (RES) {
-            Pop<ST>::st(a.fo, i * N + s, dfeq - fbar(i, r.dphi, phi, r.dp0, cu));
+            if (a.fo) Pop<ST>::st(a.fo, i * N + s, dfeq - fbar(i, r.dphi, phi, r.dp0, cu));
             Pop<ST>::st(a.go, i * N + s, dgeq - gbar(i, r.S, cu));
         } else {
-            Pop<ST>::st(a.fo, i * N + s, dfeq);
+            if (a.fo) Pop<ST>::st(a.fo, i * N + s, dfeq);
             Pop<ST>::st(a.go, i * N + s, dgeq);
         }
     }
@@ -878,14 +975,14 @@ __global__ void pops_to_host(const FastArgs a, double* __restrict__ fa, double* 
     const double E[3] = {2.0 / 9.0, 1.0 / 9.0, 1.0 / 72.0};
 #pragma unroll
     for (int i = 0; i < Q; ++i) {
-        double fv = (double)Pop<ST>::ld(a.f, i * N + s);
+        double fv = a.f ? (double)Pop<ST>::ld(a.f, i * N + s) : 0.0;
         double gv = (double)Pop<ST>::ld(a.g, i * N + s);
         if (RES) {
             const float cu = (i == 0) ? 0.f : cdot3(i, u1, u2, u3);
             fv += (double)fbar(i, dphi, phi, dp0, cu);
             gv += (double)gbar(i, S, cu);
         }
-        fa[s * Q + i] = fv + (double)a.fref[i];
+        fa[s * Q + i] = a.f ? fv + (double)a.fref[i] : 0.0;  // single phase: no f
         ga[s * Q + i] = gv + E[wclass(i)];
     }
 }
@@ -910,7 +1007,7 @@ __global__ void pops_from_host(const FastArgs a, const double* __restrict__ fa, 
         df[i] = (float)(fv - (double)a.fref[i]);
         dg[i] = (float)(gv - E[wclass(i)]);
     }
-    const float dphi = (float)(ph - (double)a.phi1);
+    const float dphi = a.fo ? (float)(ph - (double)a.phi1) : 0.f;  // single phase: phi = phi1
     const float u1 = (float)m1, u2 = (float)m2, u3 = (float)m3, dp = (float)(pp - 1.0 / 3.0);
     a.maco[s] = dphi;
     a.maco[N + s] = u1;
@@ -928,7 +1025,7 @@ __global__ void pops_from_host(const FastArgs a, const double* __restrict__ fa, 
             fv -= fbar(i, dphi, phi, dp0, cu);
             gv -= gbar(i, S, cu);
         }
-        Pop<ST>::st(a.fo, i * N + s, fv);
+        if (a.fo) Pop<ST>::st(a.fo, i * N + s, fv);
         Pop<ST>::st(a.go, i * N + s, gv);
     }
 }
@@ -986,6 +1083,7 @@ static void fill_fast(dl_handle* h, FastArgs& a) {
     a.ny = h->ny;
     a.nz = h->nz;
     a.lz = h->lz > 0 ? h->lz : 16;
+    a.l2_prefetch = h->l2_prefetch;
     a.N = (long long)h->N;
     a.st = h->d_state;
     a.phi1 = (float)P.phi1;
@@ -1003,6 +1101,7 @@ static void fill_fast(dl_handle* h, FastArgs& a) {
     a.csd = (float)(P.Cs * P.Cs * P.delta * P.delta);
     a.anu23 = (float)((2.0 / 3.0) * P.Anu);
     a.inv_ds = (float)(1.0 / P.ds);
+    a.omg_sp = 1.f / (0.5f + 3.f * a.nu1 * a.inv_ds + a.anu23);
     a.inv_lap = (float)(1.0 / (5.0 * P.ds * P.ds));
     a.inv_grad = (float)(1.0 / (10.0 * P.ds));
     const double p0ref = P.phi1 * P.T / (1.0 - P.b * P.phi1) - P.a * P.phi1 * P.phi1;
@@ -1083,10 +1182,12 @@ int fast_alloc(dl_handle* h) {
     const size_t N = h->N;
     const size_t es = (h->form == DL_FORM_FP16) ? sizeof(__half) : sizeof(float);
     for (int k = 0; k < 2; ++k) {
-        DL_CUDA(h, cudaMalloc(&h->fs[k], es * Q * N));
+        if (!h->single) {  // the single-phase step has no f
+            DL_CUDA(h, cudaMalloc(&h->fs[k], es * Q * N));
+            DL_CUDA(h, cudaMemsetAsync(h->fs[k], 0, es * Q * N, h->stream));
+        }
         DL_CUDA(h, cudaMalloc(&h->gs[k], es * Q * N));
         DL_CUDA(h, cudaMalloc(&h->mac32[k], sizeof(float) * 5 * N));
-        DL_CUDA(h, cudaMemsetAsync(h->fs[k], 0, es * Q * N, h->stream));
         DL_CUDA(h, cudaMemsetAsync(h->gs[k], 0, es * Q * N, h->stream));
         DL_CUDA(h, cudaMemsetAsync(h->mac32[k], 0, sizeof(float) * 5 * N, h->stream));
     }
@@ -1186,31 +1287,45 @@ static int fast_spectral_project(dl_handle* h) {
     return DL_OK;
 }
 
-static const int PROJ_ROWS = 64;  // rows of the band projection per block
+static const int PROJ_ROWS = 64;  // rows of the band projection per block (batched ensembles)
 
+// band projection launch: three blocks per SM (the register limit), rows
+// split evenly so that no SM runs a second wave alone
 static int launch_projection(dl_handle* h, const FastArgs& a) {
     const long long rows = (long long)a.ny * a.nz;
-    const unsigned grid = (unsigned)((rows + PROJ_ROWS - 1) / PROJ_ROWS);
-    DL_LAUNCH(h, false, (sp_project_fast<<<grid, PROJ_NT, 0, h->stream>>>(a, PROJ_ROWS)));
+    static int sm_count[64] = {0};
+    int& sms = sm_count[h->device & 63];
+    if (sms == 0 && cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device) != cudaSuccess) sms = 152;
+    const long long want = 3LL * sms;
+    const int rpb = (int)((rows + want - 1) / want);
+    const unsigned grid = (unsigned)((rows + rpb - 1) / rpb);
+    DL_LAUNCH(h, false, (sp_project_fast<<<grid, PROJ_NT, 0, h->stream>>>(a, rpb)));
     DL_CUDA(h, cudaGetLastError());
     return DL_OK;
 }
 
-template <typename ST, bool RES, bool LES, int FMODE>
+template <typename ST, bool RES, bool LES, int FMODE, bool SP = false>
 static int launch_fused(dl_handle* h, const FastArgs& a) {
     static bool configured[64] = {false};
     const int dev = h->device & 63;
     const size_t sm = smem_bytes<RES, LES, FMODE>();
     if (!configured[dev]) {
-        DL_CUDA(h, cudaFuncSetAttribute(step_fused<ST, RES, LES, FMODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)sm));
+        DL_CUDA(h, cudaFuncSetAttribute(step_fused<ST, RES, LES, FMODE, SP>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
         configured[dev] = true;
     }
     dim3 grid((a.nx + TX - 1) / TX, (a.ny + TY - 1) / TY, (a.nz + a.lz - 1) / a.lz);
-    DL_LAUNCH(h, true, (step_fused<ST, RES, LES, FMODE><<<grid, NT, sm, h->stream>>>(a)));
+    DL_LAUNCH(h, true, (step_fused<ST, RES, LES, FMODE, SP><<<grid, NT, sm, h->stream>>>(a)));
     DL_CUDA(h, cudaGetLastError());
     if (FMODE == F_SPECTRAL) return launch_projection(h, a);
     return DL_OK;
+}
+
+template <typename ST, bool RES>
+static int dispatch_single(dl_handle* h, const FastArgs& a, int fmode) {
+    if (fmode == F_SPECTRAL) return launch_fused<ST, RES, false, F_SPECTRAL, true>(h, a);
+    if (fmode == F_ARRAY) return launch_fused<ST, RES, false, F_ARRAY, true>(h, a);
+    return launch_fused<ST, RES, false, F_NONE, true>(h, a);
 }
 
 template <typename ST, bool RES>
@@ -1283,7 +1398,10 @@ int fast_step(dl_handle* h) {
     make_step_args(h, 0, a);
     const int fmode = force_fmode(h);
     const bool les = h->P.les != 0;
-    rc = (h->form == DL_FORM_FP16) ? dispatch<__half, true>(h, a, les, fmode) : dispatch<float, false>(h, a, les, fmode);
+    if (h->single)
+        rc = (h->form == DL_FORM_FP16) ? dispatch_single<__half, true>(h, a, fmode) : dispatch_single<float, false>(h, a, fmode);
+    else
+        rc = (h->form == DL_FORM_FP16) ? dispatch<__half, true>(h, a, les, fmode) : dispatch<float, false>(h, a, les, fmode);
     if (rc != DL_OK) return rc;
     advance(h, 1);
     return DL_OK;

@@ -232,7 +232,7 @@ __global__ void __launch_bounds__(256) equilibrium_fp64(const Fp64Args a) {
     for (int i = 0; i < Q; ++i) {
         double fe, ge;
         equil_fp64<ANU>(a, i, s, fe, ge);
-        a.fo[i * a.N + s] = fe;
+        if (a.fo) a.fo[i * a.N + s] = fe;
         a.go[i * a.N + s] = ge;
     }
 }
@@ -267,12 +267,12 @@ __global__ void __launch_bounds__(256) moments_kernel_fp64(const Fp64Args a) {
     double fn[Q], gn[Q];
 #pragma unroll
     for (int i = 0; i < Q; ++i) {
-        fn[i] = a.f[i * a.N + s];
+        fn[i] = a.f ? a.f[i * a.N + s] : 0.0;
         gn[i] = a.g[i * a.N + s];
     }
     double ph, pp, a1, a2, a3;
     moments_fp64(fn, gn, ph, pp, a1, a2, a3);
-    a.maco[s] = ph;
+    a.maco[s] = a.f ? ph : a.phi1;
     a.maco[a.N + s] = a1;
     a.maco[2 * a.N + s] = a2;
     a.maco[3 * a.N + s] = a3;
@@ -293,11 +293,15 @@ __global__ void __launch_bounds__(256) collide_fp64(const Fp64Args a) {
     for (int i = 0; i < Q; ++i) {
         const long long src = wrapi(x - cx(i), a.nx) +
                               (long long)a.nx * (wrapi(y - cy(i), a.ny) + (long long)a.ny * wrapi(z - cz(i), a.nz));
-        const double fs = __ldg(a.f + i * N + src);
         const double gs = __ldg(a.g + i * N + src);
         double fe, ge;
         equil_fp64<ANU>(a, i, src, fe, ge);
-        fn[i] = fs - (fs - fe) / a.tauf;
+        if (a.f) {
+            const double fs = __ldg(a.f + i * N + src);
+            fn[i] = fs - (fs - fe) / a.tauf;
+        } else {
+            fn[i] = 0.0;  // single phase: no f
+        }
         double gv = gs - (gs - ge) / __ldg(a.rec + R_TAUG * N + src);
         if (FORCE && i != 0) {
             const double cF = cdot(i, __ldg(a.force + src), __ldg(a.force + N + src), __ldg(a.force + 2 * N + src));
@@ -325,11 +329,12 @@ __global__ void __launch_bounds__(256) collide_fp64(const Fp64Args a) {
     }
     double ph, pp, a1, a2, a3;
     moments_fp64(fn, gn, ph, pp, a1, a2, a3);
+    if (!a.f) ph = a.phi1;
     bool bad = false;
     if (active) {
 #pragma unroll
         for (int i = 0; i < Q; ++i) {
-            a.fo[i * N + s] = fn[i];
+            if (a.f) a.fo[i * N + s] = fn[i];
             a.go[i * N + s] = gn[i];
         }
         a.maco[s] = ph;
@@ -393,10 +398,12 @@ int fp64_alloc(dl_handle* h) {
     const bool gradu = h->P.les || h->P.Anu != 0.0;
     h->nrec = gradu ? 20 : 11;
     for (int k = 0; k < 2; ++k) {
-        DL_CUDA(h, cudaMalloc(&h->f64[k], sizeof(double) * Q * N));
+        if (!h->single) {  // the single-phase step has no f
+            DL_CUDA(h, cudaMalloc(&h->f64[k], sizeof(double) * Q * N));
+            DL_CUDA(h, cudaMemsetAsync(h->f64[k], 0, sizeof(double) * Q * N, h->stream));
+        }
         DL_CUDA(h, cudaMalloc(&h->g64[k], sizeof(double) * Q * N));
         DL_CUDA(h, cudaMalloc(&h->mac64[k], sizeof(double) * 5 * N));
-        DL_CUDA(h, cudaMemsetAsync(h->f64[k], 0, sizeof(double) * Q * N, h->stream));
         DL_CUDA(h, cudaMemsetAsync(h->g64[k], 0, sizeof(double) * Q * N, h->stream));
         DL_CUDA(h, cudaMemsetAsync(h->mac64[k], 0, sizeof(double) * 5 * N, h->stream));
     }

@@ -176,8 +176,12 @@ class Droplet(_HandleAPI):
 
     prefix = "dl"
 
-    def __init__(self, params: Params, shape, form: int = FORM_FP64):
-        super().__init__(load(), params, shape, form)
+    def __init__(self, params: Params, shape, form: int = FORM_FP64, single_phase: bool = False):
+        """single_phase: the g-only step of the precursor turbulence program
+        (program/lbm_iht_xy.f90), DL_SINGLE_PHASE; phi is then not a field."""
+        self.single_phase = bool(single_phase)
+        super().__init__(load(), params, shape, int(form) | (_abi.DL_SINGLE_PHASE if single_phase else 0))
+        self.form = int(form)
 
     def _detail(self) -> str:
         if getattr(self, "_h", None) is None:

@@ -45,6 +45,13 @@ extern "C" {
                              deviations from the bulk equilibrium at phi1, p=1/3 */
 #define DL_FORM_FP16  16  /* FP32 arithmetic; populations stored as scaled
                              FP16 deviations; FP64 for conservation sums */
+/* OR-ed into the form: the single-phase step of the precursor turbulence
+ * program (program/lbm_iht_xy.f90: equilibrium_cal :532-559, g_cal :561-590,
+ * physics :592-654): g only, geq = E (3p + 3c.u + 4.5 (c.u)^2 - 1.5 u^2),
+ * tau_g = 1/2 + 3 nu1/ds, the same forcing and walls. No f populations are
+ * allocated; phi is not a field (dl_get_fields returns phi = phi1). Requires
+ * les = 0 and Anu = 0 (the precursor's Cs = 0). */
+#define DL_SINGLE_PHASE 0x100
 
 /* ---- body-force modes ------------------------------------------------------ */
 #define DL_FORCE_NONE      0
@@ -120,7 +127,8 @@ const char* dl_status_string(int status);
 
 /* Allocate a whole-domain state on the current CUDA device.
  * Replaces the allocations of ini/ini_op, program/lbm_drop_xy.f90:131-285,
- * without the MPI decomposition (:143-185): the domain is resident. */
+ * without the MPI decomposition (:143-185): the domain is resident.
+ * form: DL_FORM_FP64 / FP32 / FP16, optionally | DL_SINGLE_PHASE. */
 int dl_create(const dl_params* params, int nx, int ny, int nz, int form,
               dl_handle** out);
 

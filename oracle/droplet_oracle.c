@@ -78,6 +78,7 @@ struct orc_state {
     double phi_min, phi_max; /* interpolation range for the next tau_g */
     int64_t n;               /* steps taken */
     int force_mode;
+    int single;              /* the single-phase precursor step (g only) */
 };
 
 static int g_threads = 0;
@@ -686,9 +687,16 @@ int orc_set_force(orc_state* o, int mode, const double* fx, const double* fy, co
     return DL_OK;
 }
 
+static void equilibrium_single(orc_state* o);
+
 /* ini, program/lbm_drop_xy.f90:244-251, and ini_op, :254-285 */
 int orc_init_equilibrium(orc_state* o) {
     if (!o) return DL_ERR_ARG;
+    if (o->single) {  /* ini, program/lbm_iht_xy.f90:270 */
+        equilibrium_single(o);
+        memcpy(o->g, o->geq, 15 * o->N * sizeof(double));
+        return DL_OK;
+    }
     various_cal(o);
     gphi_cal(o);
     equilibrium_cal(o, o->f, o->g);
@@ -706,9 +714,81 @@ int orc_set_populations(orc_state* o, const double* f, const double* g) {
     return DL_OK;
 }
 
-/* one step = the loop body of program/lbm_drop_xy.f90:787-840 */
+/* ---- the single-phase precursor step, program/lbm_iht_xy.f90 ------------
+ * equilibrium_cal (:532-559): geq = E (3p + 3 c.u + 4.5 (c.u)^2 - 1.5 u^2) */
+static void equilibrium_single(orc_state* o) {
+    const size_t N = o->N;
+#pragma omp parallel for schedule(static)
+    for (size_t s = 0; s < N; ++s) {
+        const double p = o->p[s], u1 = o->u1[s], u2 = o->u2[s], u3 = o->u3[s];
+        for (int i = 0; i < 15; ++i) {
+            const double cu = u1 * (double)CX[i] + u2 * (double)CY[i] + u3 * (double)CZ[i];
+            o->geq[15 * s + i] = EW[i] * (3.0 * p + 3.0 * cu + 4.5 * (cu * cu) - 1.5 * (u1 * u1 + u2 * u2 + u3 * u3));
+        }
+    }
+}
+
+/* g_cal (:561-590) with tau_g = 1/2 + 3 (nu + nue)/ds, nue = 0 (Cs = 0, :21-22,
+ * physics :649), then physics (:592-654): copy and moments p = sum g/3, u = sum c g */
+static void step_single(orc_state* o) {
+    const double taug = 0.5 + 3.0 * (o->P.nu1 + 0.0) / o->P.ds;
+    const double ds3 = 3.0 * o->P.ds;
+    const int nx = o->nx, ny = o->ny, nz = o->nz;
+    equilibrium_single(o);
+#pragma omp parallel for schedule(static)
+    for (int z = 0; z < nz; ++z)
+        for (int y = 0; y < ny; ++y)
+            for (int x = 0; x < nx; ++x) {
+                size_t s = sidx(o, x, y, z);
+                for (int i = 0; i < 15; ++i) {
+                    size_t n = nbr(o, x, y, z, -CX[i], -CY[i], -CZ[i]);
+                    double gs = o->g[15 * n + i];
+                    o->gnext[15 * s + i] =
+                        gs - (gs - o->geq[15 * n + i]) / taug +
+                        ds3 * EW[i] *
+                            ((double)CX[i] * o->fx[n] + (double)CY[i] * o->fy[n] + (double)CZ[i] * o->fz[n]);
+                }
+            }
+}
+
+static void physics_single(orc_state* o) {
+    const size_t N = o->N;
+#pragma omp parallel for schedule(static)
+    for (size_t s = 0; s < N; ++s) {
+        double pp = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+        for (int i = 0; i < 15; ++i) {
+            const double gv = o->gnext[15 * s + i];
+            o->g[15 * s + i] = gv;
+            pp = pp + gv / 3.0;
+            a1 = a1 + (double)CX[i] * gv;
+            a2 = a2 + (double)CY[i] * gv;
+            a3 = a3 + (double)CZ[i] * gv;
+        }
+        o->p[s] = pp;
+        o->u1[s] = a1;
+        o->u2[s] = a2;
+        o->u3[s] = a3;
+    }
+}
+
+int orc_set_single(orc_state* o, int on) {
+    if (!o) return DL_ERR_ARG;
+    o->single = on ? 1 : 0;
+    return DL_OK;
+}
+
+/* one step = the loop body of program/lbm_drop_xy.f90:787-840, or of
+ * program/lbm_iht_xy.f90:960-980 in the single-phase mode */
 static void step_once(orc_state* o) {
     int64_t n = o->n + 1;
+    if (o->single) {
+        if (o->force_mode == DL_FORCE_SPECTRAL) spectral_force(o);
+        step_single(o);
+        if (o->P.walls) bounce_back(o, n);
+        physics_single(o);
+        o->n = n;
+        return;
+    }
     if (o->force_mode == DL_FORCE_SPECTRAL) spectral_force(o);
     various_cal(o);
     gphi_cal(o);

@@ -29,6 +29,9 @@ int orc_init_equilibrium(orc_state* o);
 int orc_set_force(orc_state* o, int mode, const double* fx, const double* fy,
                   const double* fz);
 int orc_step(orc_state* o, int nsteps);
+/* Nonzero: the single-phase precursor step of program/lbm_iht_xy.f90 (g only,
+ * tau_g = 1/2 + 3 nu1/ds); set before orc_init_equilibrium. */
+int orc_set_single(orc_state* o, int on);
 int orc_get_fields(orc_state* o, double* phi, double* u1, double* u2,
                    double* u3, double* p);
 int orc_get_populations(orc_state* o, double* f, double* g);

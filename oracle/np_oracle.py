@@ -177,3 +177,63 @@ class NumpyStep:
     def populations(self):
         """f, g with shape (nz, ny, nx, 15) like the C-ABI."""
         return np.stack(self.f, axis=-1), np.stack(self.g, axis=-1)
+
+
+class SinglePhaseStep:
+    """The single-phase step of the precursor turbulence program
+    program/lbm_iht_xy.f90: equilibrium_cal (:532-559), g_cal (:561-590) and
+    physics (:592-654), in the reference's evaluation order. tau_g is
+    1/2 + 3 (nu + nu_t)/ds with nu_t = 0 (the program's Cs = 0, :21-22)."""
+
+    def __init__(self, nu, fields, ds=1.0):
+        self.nu, self.ds = nu, ds
+        self.u = [fields["u1"].astype(np.float64).copy(), fields["u2"].astype(np.float64).copy(),
+                  fields["u3"].astype(np.float64).copy()]
+        self.p = fields["p"].astype(np.float64).copy()
+        self.force = [np.zeros_like(self.p) for _ in range(3)]
+        self.g = None
+
+    # equilibrium_cal, :532-559
+    def equilibria(self):
+        u1, u2, u3 = self.u
+        p = self.p
+        geq = []
+        for i in range(15):
+            cu = u1 * float(CX[i]) + u2 * float(CY[i]) + u3 * float(CZ[i])
+            geq.append(E[i] * (3.0 * p + 3.0 * cu + 4.5 * (cu * cu) - 1.5 * (u1 * u1 + u2 * u2 + u3 * u3)))
+        return geq
+
+    # ini, :270
+    def init_equilibrium(self):
+        self.g = self.equilibria()
+
+    def step(self, nsteps=1):
+        for _ in range(nsteps):
+            self._step()
+
+    def _step(self):
+        taug = 0.5 + 3.0 * (self.nu + 0.0) / self.ds  # physics :649
+        geq = self.equilibria()
+        fx, fy, fz = self.force
+        gn = []
+        # g_cal, :573-582
+        for i in range(15):
+            gs = shifted(self.g[i], i, -1)
+            gn.append(gs - (gs - shifted(geq[i], i, -1)) / taug
+                      + 3.0 * self.ds * E[i] * (float(CX[i]) * shifted(fx, i, -1) + float(CY[i]) * shifted(fy, i, -1)
+                                                + float(CZ[i]) * shifted(fz, i, -1)))
+        # physics, :613-625
+        p = np.zeros_like(self.p)
+        u = [np.zeros_like(self.p) for _ in range(3)]
+        for i in range(15):
+            p = p + gn[i] / 3.0
+            u[0] = u[0] + float(CX[i]) * gn[i]
+            u[1] = u[1] + float(CY[i]) * gn[i]
+            u[2] = u[2] + float(CZ[i]) * gn[i]
+        self.g, self.p, self.u = gn, p, u
+
+    def fields(self):
+        return dict(u1=self.u[0], u2=self.u[1], u3=self.u[2], p=self.p)
+
+    def populations(self):
+        return np.stack(self.g, axis=-1)

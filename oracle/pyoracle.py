@@ -56,8 +56,12 @@ class OracleDroplet(_HandleAPI):
 
     prefix = "orc"
 
-    def __init__(self, params, shape, form=None):
+    def __init__(self, params, shape, form=None, single_phase=False):
         super().__init__(load(), params, shape, form)
+        self.single_phase = bool(single_phase)
+        if single_phase:
+            self._lib.orc_set_single.argtypes = [C.c_void_p, C.c_int]
+            self._call("set_single", 1)
 
     def get_force(self):
         out = [np.empty(self.shape3) for _ in range(3)]

@@ -201,3 +201,73 @@ def test_taylor_green_decay_rate():
     amp = np.sum(a * np.sin(k * y)) / np.sum(np.sin(k * y) ** 2)
     expect = U * np.exp(-nu * k * k * t)
     assert abs(amp / expect - 1.0) < 0.02
+
+
+def single_phase_params(**kw):
+    """The two-phase parameters that reduce the g update to the precursor's
+    single-phase step: no interface terms, one viscosity, fixed range."""
+    base = dict(kappaf=0.0, kappag=0.0, nu1=0.02, nu2=0.02, Anu=0.0, visc_mode=_abi.DL_VISC_FIXED)
+    base.update(kw)
+    return Params.lbm_drop_xy().replace(**base)
+
+
+@pytest.mark.parametrize("forced", [False, True])
+def test_single_phase_restatement_equals_c_oracle_g_update(forced):
+    """program/lbm_iht_xy.f90's g-only step (NumPy restatement) equals the C
+    oracle's g update with kappaf = kappag = Anu = 0 and nu2 = nu1, bit for
+    bit: p, u and g."""
+    shape = (10, 9, 8)
+    nx, ny, nz = shape
+    P = single_phase_params()
+    rng = np.random.default_rng(5)
+    u = [0.02 * rng.standard_normal((nz, ny, nx)) for _ in range(3)]
+    f = init_fields.fields(np.full((nz, ny, nx), P.phi1), *u)
+    f["p"] = f["p"] + 1e-3 * rng.standard_normal((nz, ny, nx))
+    force = None
+    if forced:
+        force = [1e-4 * np.sin(np.arange(nx) * 0.7)[None, None, :] * np.ones((nz, ny, nx)),
+                 np.full((nz, ny, nx), 3e-5),
+                 1e-4 * np.cos(np.arange(nz) * 0.5)[:, None, None] * np.ones((nz, ny, nx))]
+    o = pyoracle.OracleDroplet(P, shape)
+    o.set_fields(**f)
+    o.init_equilibrium()
+    s = np_oracle.SinglePhaseStep(P.nu1, f, ds=P.ds)
+    s.init_equilibrium()
+    if force is not None:
+        o.set_force(_abi.DL_FORCE_STATIC, *force)
+        s.force = [np.asarray(a, dtype=np.float64) for a in force]
+    o.step(7)
+    s.step(7)
+    fo, fs = o.get_fields(), s.fields()
+    for k in ("u1", "u2", "u3", "p"):
+        assert np.array_equal(fo[k], fs[k]), k
+    assert np.array_equal(o.get_populations()[1], s.populations())
+
+
+@pytest.mark.parametrize("forced", [False, True])
+def test_c_single_phase_mode_equals_numpy_restatement(forced):
+    """The C oracle's own single-phase mode (the CPU baseline of the precursor
+    workload) against the NumPy restatement of program/lbm_iht_xy.f90."""
+    shape = (10, 9, 8)
+    nx, ny, nz = shape
+    P = single_phase_params(eps=1e-6, kc=3)
+    rng = np.random.default_rng(9)
+    u = [0.02 * rng.standard_normal((nz, ny, nx)) for _ in range(3)]
+    f = init_fields.fields(np.full((nz, ny, nx), P.phi1), *u)
+    o = pyoracle.OracleDroplet(P, shape, single_phase=True)
+    o.set_fields(**f)
+    o.init_equilibrium()
+    s = np_oracle.SinglePhaseStep(P.nu1, f, ds=P.ds)
+    s.init_equilibrium()
+    if forced:
+        force = [1e-4 * np.sin(np.arange(nx) * 0.7)[None, None, :] * np.ones((nz, ny, nx)),
+                 np.full((nz, ny, nx), 3e-5),
+                 1e-4 * np.cos(np.arange(nz) * 0.5)[:, None, None] * np.ones((nz, ny, nx))]
+        o.set_force(_abi.DL_FORCE_STATIC, *force)
+        s.force = force
+    o.step(5)
+    s.step(5)
+    fo, fs = o.get_fields(), s.fields()
+    for k in ("u1", "u2", "u3", "p"):
+        assert np.array_equal(fo[k], fs[k]), k
+    assert np.array_equal(o.get_populations()[1], s.populations())
