@@ -147,6 +147,34 @@ def new_sim(w, rank: int = 0):
     return sim
 
 
+def phi_error(w, steps: int, stream_ptr: int):
+    """The stated error of the reduced-precision form: the same workload (full
+    size, same seed) run `steps` steps in the plain FP64 form and in the chosen
+    form on this GPU; max |phi~ difference| (phi~ = 2 (phi - phi1)/(phi2 - phi1) - 1)
+    and max |u| difference."""
+    import numpy as np
+    from droplet_gb300.solver import Droplet
+
+    out = {}
+    for form in (64, w.form):
+        d = Droplet(w.params, w.shape, form, single_phase=w.single_phase)
+        d.set_stream(stream_ptr)
+        d.set_fields(**w.fields)
+        d.init_equilibrium()
+        d.set_force(w.force_mode)
+        d.step(steps)
+        out[form] = d.get_fields()
+        d.close()
+    a, b = out[w.form], out[64]
+    span = w.params.phi2 - w.params.phi1
+    res = {"vs": "plain FP64 form on the GPU", "steps": steps,
+           "u_max": float(max(np.abs(a[k] - b[k]).max() for k in ("u1", "u2", "u3"))),
+           "p_max": float(np.abs(a["p"] - b["p"]).max())}
+    if not w.single_phase:
+        res["phi_tilde_max"] = float(2.0 * np.abs(a["phi"] - b["phi"]).max() / span)
+    return res
+
+
 def cpu_baseline(w, budget_s: float = 15.0, threads: int | None = None):
     """Oracle (OpenMP restatement) MLUPS on this host on a bounded sample of
     the workload: the full domain when a step fits the budget, else a slab."""
@@ -347,6 +375,10 @@ def run_ours(args):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(w, budget_s=args.cpu_budget)
 
+    accuracy = None
+    if rank == 0 and form != 64 and args.accuracy_steps > 0:
+        accuracy = phi_error(w, args.accuracy_steps, stream.cuda_stream)
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -359,6 +391,7 @@ def run_ours(args):
                        "notes": w.notes,
                        "tune": None if tune is None else {k: v for k, v in tune.items() if k != "timings"}},
             "roofline": roofline,
+            "accuracy": accuracy,
             "cpu_baseline": cpu,
             "e2e": e2e,
             "clocks": clk,
@@ -507,6 +540,8 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--members", type=int, default=64)
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch shape")
+    ap.add_argument("--accuracy-steps", type=int, default=500,
+                    help="steps of the FP64-form comparison that states the phi error (0: skip)")
     ap.add_argument("--diag-every", type=int, default=100, help="steps between whole-domain diagnostics in e2e")
     args = ap.parse_args()
     if args.warmup < 3:

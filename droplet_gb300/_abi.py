@@ -102,6 +102,14 @@ class DLDiag(C.Structure):
         return out
 
 
+class DLEnergyDiag(C.Structure):
+    _fields_ = [("psi_sum", C.c_double), ("mu_sum", C.c_double), ("grad_sq_sum", C.c_double),
+                ("spectrum_sum", C.c_double), ("nbins", C.c_int64), ("step", C.c_int64)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class DLProfileStats(C.Structure):
     _fields_ = [
         ("main_ms", C.c_double),
@@ -146,6 +154,8 @@ def declare(lib: C.CDLL, prefix: str) -> None:
         lib.dl_set_stream.restype = C.c_int
         lib.dl_reduce.argtypes = [h, C.POINTER(DLDiag)]
         lib.dl_reduce.restype = C.c_int
+        lib.dl_energy.argtypes = [h, C.POINTER(DLEnergyDiag), C.c_void_p, C.c_int64]
+        lib.dl_energy.restype = C.c_int
         lib.dl_reduce_static.argtypes = [h, C.c_int, C.POINTER(DLDiag)]
         lib.dl_reduce_static.restype = C.c_int
         lib.dl_sync.argtypes = [h]
@@ -220,6 +230,7 @@ HEADER_SYMBOLS = [
     "dl_get_minmax",
     "dl_reduce",
     "dl_reduce_static",
+    "dl_energy",
     "dl_sync",
     "dl_last_error",
     "dl_profile",

@@ -43,6 +43,7 @@ SOURCES = {
     "layout.cu": EXACT,
     "reduce.cu": EXACT,
     "reduce_static.cu": EXACT,
+    "energy.cu": EXACT,
     "step_fast.cu": FAST,
     "adjoint.cu": FAST,
     "labels.cu": FAST,
@@ -92,7 +93,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     with cf.ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
         objs = list(ex.map(lambda s: _compile(nvcc, s[0], s[1], verbose), srcs))
     tmp = LIB + ".tmp"
-    cmd = [nvcc] + ARCH + ["-shared", "-o", tmp] + objs
+    cmd = [nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcufft"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

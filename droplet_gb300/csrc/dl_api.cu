@@ -198,6 +198,7 @@ int dl_destroy(dl_handle* h) {
     cudaFree(h->d_state);
     cudaFree(h->d_diag);
     cudaFree(h->lbl_buf);
+    energy_free(h);
     prof_release(h);
     delete h;
     return DL_OK;
@@ -533,6 +534,12 @@ int dl_sync(dl_handle* h) {
     DL_CUDA(h, cudaMemcpy(&s, h->d_state, sizeof(s), cudaMemcpyDeviceToHost));
     if (s.nan_flag) return set_error(h, DL_ERR_NAN, "non-finite phi/u/p first seen at step %lld", s.nan_step);
     return DL_OK;
+}
+
+int dl_energy(dl_handle* h, dl_energy_diag* out, double* spectrum, int64_t nbins) {
+    if (!h || !out) return DL_ERR_ARG;
+    if (!h->fields_set) return set_error(h, DL_ERR_STATE, "dl_energy before dl_set_fields");
+    return energy_diagnostics(h, out, spectrum, (long long)nbins);
 }
 
 int dl_reduce(dl_handle* h, dl_diag* out) {

@@ -137,6 +137,11 @@ struct dl_handle {
     float* force32;          // [3][N]
     int lz;                  // z planes per block of the fused kernel
     int l2_prefetch;         // fused kernel: bulk L2 prefetch of the next plane's pulls
+    // dl_energy: cuFFT plan and buffers (allocated on first use)
+    long long en_plan;
+    int en_plan_ok;
+    double* en_buf;
+    size_t en_bytes;
 
     dl::SpectralPlan sp;
     dl::FastSpectral fsp;
@@ -206,6 +211,8 @@ int adjoint_grads(dl_handle* h, double* out4);
 int soa_to_aos(dl_handle* h, const double* d_soa, double* d_aos);
 int aos_to_soa(dl_handle* h, const double* d_aos, double* d_soa);
 int fill_doubles(dl_handle* h, double* d, double v, size_t n);
+int energy_diagnostics(dl_handle* h, dl_energy_diag* out, double* spectrum_host, long long nbins);
+void energy_free(dl_handle* h);
 // diagnostics (reduce.cu)
 int reduce_fields(dl_handle* h, const double* d_mac, dl_diag* out);
 int reduce_fields_f32(dl_handle* h, const float* d_mac, dl_diag* out);

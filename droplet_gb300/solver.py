@@ -202,6 +202,18 @@ class Droplet(_HandleAPI):
         self._call("reduce", C.byref(d))
         return d.as_dict()
 
+    def energy(self, nbins: int | None = None):
+        """In-situ energy diagnostics (dl_energy): dict of the free-energy sums
+        and, unless nbins == 0, the kinetic-energy spectrum (nbins defaults to
+        the reference's nx/2 + 1 bins)."""
+        nb = self.nx // 2 + 1 if nbins is None else int(nbins)
+        spec = np.zeros(max(nb, 1), dtype=np.float64)
+        d = _abi.DLEnergyDiag()
+        self._call("energy", C.byref(d), _ptr(spec) if nb > 0 else None, C.c_int64(nb))
+        out = d.as_dict()
+        out["spectrum"] = spec[:nb].copy()
+        return out
+
     def reduce_static(self, nblocks: int = 0) -> dict:
         """The diagnostics of reduce() through dl_reduce_static, which
         allocates no device memory (fixed scratch inside the library, shared

@@ -108,6 +108,19 @@ typedef struct dl_diag {
     int32_t pad_;
 } dl_diag;
 
+/* In-situ energy diagnostics of the current fields (dl_energy). */
+typedef struct dl_energy_diag {
+    double psi_sum;      /* sum of phi T ln(phi/(1 - b phi)) - a phi^2: free_energy_cal,
+                            program/energy_budget.f90:1012-1023 */
+    double mu_sum;       /* sum of the chemical potential T ln(phi/(1 - b phi))
+                            + T/(1 - b phi) - 2 a phi - kappag lap(phi):
+                            chemical_potencial_cal, program/energy_budget.f90:998-1010 */
+    double grad_sq_sum;  /* sum of |grad phi|^2 (14-neighbour stencil) */
+    double spectrum_sum; /* sum of the returned spectrum bins */
+    int64_t nbins;       /* bins returned */
+    int64_t step;
+} dl_energy_diag;
+
 /* Launch accounting of the library's own kernels (for benchmarks). */
 typedef struct dl_profile_stats {
     double main_ms;          /* summed device time of the fused step kernel */
@@ -188,6 +201,16 @@ int dl_get_minmax(dl_handle* h, double* phi_min, double* phi_max);
  * analysis programs (kinetic.d in program/lbm_iht_xy.f90:777-822, the
  * droplet moments of prototype_program/two-phase/drop8_mpi.f90:812-970). */
 int dl_reduce(dl_handle* h, dl_diag* out);
+
+/* In-situ turbulence and free-energy diagnostics: the sums of dl_energy_diag
+ * and, when nbins > 0, the kinetic-energy spectrum of enesupe_cal
+ * (program/turbulence_hit_xy.f90:588-645) in spectrum[0..nbins): bin j holds
+ * the modes with int(|k|) = j (the reference's k_index = j + 1), summed over
+ * k1 in [0,nx), k2 in [0,ny), k3 in [0,nz/2] of 0.5 |u_hat|^2 with weight 1 at
+ * k3 = 0 and 2 elsewhere, u_hat = FFT(u)/N. The reference's array has
+ * nx/2 + 1 bins; modes beyond nbins are left out. FP64 FFTs (cuFFT); the
+ * first call plans the transform and allocates its buffers. */
+int dl_energy(dl_handle* h, dl_energy_diag* out, double* spectrum, int64_t nbins);
 
 /* dl_reduce_static: the same diagnostics as dl_reduce, for callers that must
  * not allocate device memory once their run is set up -- a host program that
