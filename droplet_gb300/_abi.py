@@ -176,6 +176,10 @@ def declare(lib: C.CDLL, prefix: str) -> None:
         lib.dl_state_floats.restype = C.c_int
         lib.dl_save_state.argtypes = [h, _vp]
         lib.dl_save_state.restype = C.c_int
+        lib.dl_adjoint_state_floats.argtypes = [h, C.POINTER(C.c_int64)]
+        lib.dl_adjoint_state_floats.restype = C.c_int
+        lib.dl_save_adjoint_state.argtypes = [h, _vp]
+        lib.dl_save_adjoint_state.restype = C.c_int
         lib.dl_load_state.argtypes = [h, _vp]
         lib.dl_load_state.restype = C.c_int
         lib.dl_adjoint_begin.argtypes = [h, _vp]
@@ -241,6 +245,8 @@ HEADER_SYMBOLS = [
     "dl_state_floats",
     "dl_save_state",
     "dl_load_state",
+    "dl_adjoint_state_floats",
+    "dl_save_adjoint_state",
     "dl_adjoint_begin",
     "dl_adjoint_step",
     "dl_adjoint_init",

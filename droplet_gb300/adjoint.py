@@ -64,10 +64,31 @@ class AdjointTiming:
         return self.backward_s / self.forward_s if self.forward_s > 0 else float("nan")
 
 
-class CheckpointedRun:
-    """Forward and reverse passes of one FP32 run with sqrt(n) checkpoints."""
+def deformation_from_diag(d: dict, phi1: float, phi2: float):
+    """D and the eigen data of the covariance of w from the device moments
+    of dl_reduce (w_sum, w_x, w_xx = xx, yy, zz, xy, xz, yz)."""
+    W = d["w_sum"]
+    m = np.array(d["w_x"]) / W
+    xx = np.array(d["w_xx"]) / W
+    Cm = np.array([[xx[0], xx[3], xx[4]], [xx[3], xx[1], xx[5]], [xx[4], xx[5], xx[2]]]) - np.outer(m, m)
+    lam, vec = np.linalg.eigh(Cm)
+    la, lb = lam[-1], lam[0]
+    A, B = math.sqrt(la), math.sqrt(lb)
+    return (A - B) / (A + B), dict(W=W, m=m, la=la, lb=lb, va=vec[:, -1], vb=vec[:, 0], A=A, B=B)
 
-    def __init__(self, params: Params, shape, u0, p0, nsteps: int, segment: int | None = None):
+
+class CheckpointedRun:
+    """Forward and reverse passes of one FP32 run. When the per-step adjoint
+    states of the whole run fit in `memory_fraction` of the free device memory
+    (20 FP32 values per site and step; 35 GB for 500 steps of 96^3), the
+    forward keeps all of them and the reverse pass recomputes nothing;
+    otherwise it keeps a full state every S = ceil(sqrt(n)) steps and
+    recomputes each segment once. The loss and its gradient stay on the
+    device: D comes from the moments of dl_reduce, dD/dphi is formed from the
+    coordinates and the eigen data."""
+
+    def __init__(self, params: Params, shape, u0, p0, nsteps: int, segment: int | None = None,
+                 memory_fraction: float = 0.6):
         import torch
 
         self.torch = torch
@@ -76,71 +97,102 @@ class CheckpointedRun:
         self.u0 = [np.ascontiguousarray(u, dtype=np.float64) for u in u0]
         self.p0 = np.ascontiguousarray(p0, dtype=np.float64)
         self.nsteps = int(nsteps)
-        self.S = int(segment or max(1, math.ceil(math.sqrt(self.nsteps))))
         self.timing = AdjointTiming()
         self.sim = None
+        self._seg = None
+        self.store_all = False
+        if segment is None:
+            nx, ny, nz = self.shape
+            need = self.nsteps * 20 * nx * ny * nz * 4
+            free, _ = torch.cuda.mem_get_info()
+            self.store_all = need <= memory_fraction * free
+            segment = self.nsteps if self.store_all else max(1, math.ceil(math.sqrt(self.nsteps)))
+        self.S = int(segment)
 
-    def _state_buffer(self):
+    def _buffer(self, kind: str):
         n = C.c_int64()
-        rc = self.sim._lib.dl_state_floats(self.sim._h, C.byref(n))
+        fn = self.sim._lib.dl_state_floats if kind == "full" else self.sim._lib.dl_adjoint_state_floats
+        rc = fn(self.sim._h, C.byref(n))
         if rc:
-            raise RuntimeError(f"dl_state_floats: {rc}")
+            raise RuntimeError(f"state size: {rc}")
         return self.torch.empty(int(n.value), dtype=self.torch.float32, device="cuda")
-
-    def _save(self, buf):
-        self.sim._call("save_state", C.c_void_p(buf.data_ptr()))
-
-    def _load(self, buf):
-        self.sim._call("load_state", C.c_void_p(buf.data_ptr()))
 
     def forward(self, phi0: np.ndarray) -> float:
         torch = self.torch
+        torch.cuda.synchronize()
         t0 = time.perf_counter()
-        if self.sim is not None:
-            self.sim.close()
-        self.sim = Droplet(self.params, self.shape, FORM_FP32)
+        if self.sim is None:
+            self.sim = Droplet(self.params, self.shape, FORM_FP32)
+            nck = 1 if self.store_all else (self.nsteps + self.S - 1) // self.S
+            self.ckpt = [self._buffer("full") for _ in range(nck)]
+            if self.store_all:
+                n = self._buffer("adjoint").numel()
+                self._all = torch.empty((self.nsteps, n), dtype=torch.float32, device="cuda")
+        self.sim.step_count = 0
         self.sim.set_fields(phi0, self.u0[0], self.u0[1], self.u0[2], self.p0)
         self.sim.init_equilibrium()
-        self.ckpt = []
         for k in range(self.nsteps):
             if k % self.S == 0:
-                b = self._state_buffer()
-                self._save(b)
-                self.ckpt.append(b)
+                self.sim._call("save_state", C.c_void_p(self.ckpt[k // self.S].data_ptr()))
+            if self.store_all:
+                self.sim._call("save_adjoint_state", C.c_void_p(self._all[k].data_ptr()))
             self.sim.step(1)
-        f = self.sim.get_fields()
-        torch.cuda.synchronize()
-        self.timing.forward_s = time.perf_counter() - t0
-        self.phi_final = f["phi"]
-        D, self.dD_dphi = deformation_and_grad(f["phi"], self.params.phi1, self.params.phi2)
+        D, self.eig = deformation_from_diag(self.sim.reduce(), self.params.phi1, self.params.phi2)
         self.D = D
+        self.timing.forward_s = time.perf_counter() - t0
         return D
 
-    def backward(self, dD_dphi: np.ndarray | None = None):
-        """Returns dict with dphi0 (array), dkappaf, dkappag, dtauf, dU."""
+    def loss_gradient(self):
+        """dD/dphi at the final step as a device tensor (N floats, x fastest)."""
         torch = self.torch
+        e = self.eig
+        nx, ny, nz = self.shape
+        dev = "cuda"
+        X = torch.arange(nx, device=dev, dtype=torch.float64).view(1, 1, nx) - e["m"][0]
+        Y = torch.arange(ny, device=dev, dtype=torch.float64).view(1, ny, 1) - e["m"][1]
+        Z = torch.arange(nz, device=dev, dtype=torch.float64).view(nz, 1, 1) - e["m"][2]
+        pa = X * e["va"][0] + Y * e["va"][1] + Z * e["va"][2]
+        pb = X * e["vb"][0] + Y * e["vb"][1] + Z * e["vb"][2]
+        A, B = e["A"], e["B"]
+        dla = (2 * B / (A + B) ** 2) / (2 * A)
+        dlb = (-2 * A / (A + B) ** 2) / (2 * B)
+        g = (dla * (pa * pa - e["la"]) + dlb * (pb * pb - e["lb"])) / e["W"] / (self.params.phi2 - self.params.phi1)
+        return g.to(torch.float32).reshape(-1).contiguous()
+
+    def backward(self, dD_dphi=None, download: bool = True):
+        """Returns dict with dphi0 (array, or device tensor when download is
+        False), dkappaf, dkappag, dtauf, dmobility, dU."""
+        torch = self.torch
+        torch.cuda.synchronize()
         t0 = time.perf_counter()
-        g = self.dD_dphi if dD_dphi is None else dD_dphi
-        lphi = torch.tensor(np.ascontiguousarray(g, dtype=np.float32).reshape(-1), device="cuda")
+        if dD_dphi is None:
+            lphi = self.loss_gradient()
+        else:
+            lphi = torch.as_tensor(np.ascontiguousarray(dD_dphi, dtype=np.float32).reshape(-1), device="cuda")
         self.sim._call("adjoint_begin", C.c_void_p(lphi.data_ptr()))
-        nseg = len(self.ckpt)
-        seg_states = [self._state_buffer() for _ in range(self.S)]
-        for j in reversed(range(nseg)):
+        if self.store_all:
+            for k in range(self.nsteps - 1, -1, -1):
+                self.sim._call("adjoint_step", C.c_void_p(self._all[k].data_ptr()), C.c_int64(k + 1))
+        elif self._seg is None:
+            self._seg = [self._buffer("adjoint") for _ in range(self.S)]
+        seg = self._seg
+        for j in ([] if self.store_all else reversed(range(len(self.ckpt)))):
             s0 = j * self.S
             s1 = min(s0 + self.S, self.nsteps)
-            self._load(self.ckpt[j])
+            self.sim._call("load_state", C.c_void_p(self.ckpt[j].data_ptr()))
             self.sim.step_count = s0
-            seg_states[0].copy_(self.ckpt[j])
-            for k in range(s0, s1 - 1):
-                self.sim.step(1)
-                self._save(seg_states[k + 1 - s0])
+            for k in range(s0, s1):
+                self.sim._call("save_adjoint_state", C.c_void_p(seg[k - s0].data_ptr()))
+                if k < s1 - 1:
+                    self.sim.step(1)
             for k in range(s1 - 1, s0 - 1, -1):
-                self.sim._call("adjoint_step", C.c_void_p(seg_states[k - s0].data_ptr()), C.c_int64(k + 1))
+                self.sim._call("adjoint_step", C.c_void_p(seg[k - s0].data_ptr()), C.c_int64(k + 1))
         out = torch.empty(self.sim.n_sites, dtype=torch.float32, device="cuda")
         self.sim._call("adjoint_init", C.c_void_p(self.ckpt[0].data_ptr()), C.c_void_p(out.data_ptr()))
         grads = (C.c_double * 4)()
         self.sim._call("adjoint_grads", grads)
-        dphi0 = out.double().cpu().numpy().reshape(self.shape[2], self.shape[1], self.shape[0])
+        nz3 = (self.shape[2], self.shape[1], self.shape[0])
+        dphi0 = out.double().cpu().numpy().reshape(nz3) if download else out.view(nz3)
         torch.cuda.synchronize()
         self.timing.backward_s = time.perf_counter() - t0
         return {"dphi0": dphi0, "dkappaf": grads[0], "dkappag": grads[1], "dtauf": grads[2],
@@ -150,6 +202,9 @@ class CheckpointedRun:
         if self.sim is not None:
             self.sim.close()
             self.sim = None
+        self.ckpt = []
+        self._seg = None
+        self._all = None
 
 
 def _function():
@@ -170,10 +225,10 @@ def _function():
 
         @staticmethod
         def backward(ctx, gD):
-            g = ctx.run.backward()
+            g = ctx.run.backward(download=False)
             ctx.run.close()
             s = gD.to(torch.float64)
-            dphi0 = torch.tensor(g["dphi0"], device=ctx.device) * s
+            dphi0 = g["dphi0"].to(device=ctx.device, dtype=torch.float64) * s
             mk = lambda v: (torch.tensor(v, dtype=torch.float64, device=ctx.device) * s)  # noqa: E731
             return dphi0, mk(g["dkappaf"]), mk(g["dkappag"]), mk(g["dtauf"]), mk(g["dU"]), None
 

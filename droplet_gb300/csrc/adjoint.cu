@@ -15,13 +15,14 @@
 //   phi = sum f, p = sum g / 3, u = sum c g.
 // Reverse of one step = three launches:
 //   adj_walls   reflected adjoints at the wall planes, d/dU;
-//   adj_local   per source site y: gather a_i = lf'_i(y + c_i), b_i = lg'_i(y + c_i),
-//               lf_i(y) = (1-wf) a_i, lg_i(y) = (1-wg) b_i, and the local adjoints
-//               of phi, A (-> lap, |grad|^2), grad phi, u, p; d/dkf, d/dkg, d/dwf;
-//   adj_stencil per site x: transpose of the lap/grad stencils, then the moments:
-//               lf_i += lphi, lg_i += lp/3 + c_i.lu.
-// The FP32 state layout is that of the FP32 form: df[15][N], dg[15][N] (deviations
-// from the bulk equilibrium) and dphi, u1, u2, u3, dp [5][N].
+//   adj_local   per source site y: gather a_i = lf'_i(y + c_i), b_i = lg'_i(y + c_i)
+//               and form the local adjoints of phi, A (-> lap, |grad|^2), grad phi,
+//               u, p; d/dkf, d/dkg, d/dwf;
+//   adj_stencil per site x: transpose of the lap/grad stencils, then
+//               lf_i = (1-wf) a_i + lphi, lg_i = (1-wg) b_i + lp/3 + c_i.lu.
+// States are in the FP32 form's layout: df[15][N] (deviations from the bulk
+// equilibrium) followed by dphi, u1, u2, u3, dp [5][N] (the adjoint state), or
+// df, dg[15][N], fields (the full state of the initial step).
 #include "dl_internal.cuh"
 #include "dl_device.cuh"
 
@@ -33,17 +34,20 @@ namespace dl {
 struct AdjArgs {
     int nx, ny, nz;
     unsigned N;
-    const float* st;      // forward state before the step: df[15N], dg[15N], mac[5N]
+    const float* st;      // forward f before the step: df[15N]
+    const float* mac;     // forward fields before the step: [5][N]
     const float* lin;     // adjoint of the post-step populations, [30][N] (f then g)
     float* lout;          // adjoint of the pre-step populations, [30][N]
     float* aux;           // [9][N]: lphi_loc, llap, lgrad x y z, lp, lu x y z
-    double* grads;        // [4]: d/dkf, d/dkg, d/dwf, d/dU
+    double* grads;        // [ADJ_NREP][4]: d/dkf, d/dkg, d/dwf, d/dU (block b adds to copy b % ADJ_NREP)
     float phi1, omf, omg, kf, kf6, kg, T, a, b, inv_lap, inv_grad;
     float fref[Q];
     float wbot[5], wtop[5];   // d g'_i / dU at the bottom / top wall, per reflected pair
     int walls_on;             // the walls moved in this step
     int stream;               // 1: a time step; 0: the initial f = feq, g = geq
 };
+
+constexpr int ADJ_NREP = 64;  // copies of the gradient accumulators (spreads the atomics)
 
 __device__ __forceinline__ int pmodi(int v, int n) {
     v %= n;
@@ -98,7 +102,7 @@ __global__ void adj_walls(AdjArgs a) {
         }
     }
     double v[1] = {dU};
-    block_add<1>(v, a.grads + 3);
+    block_add<1>(v, a.grads + 4 * (blockIdx.x % ADJ_NREP) + 3);
 }
 
 __global__ void __launch_bounds__(256) adj_local(AdjArgs a) {
@@ -107,7 +111,7 @@ __global__ void __launch_bounds__(256) adj_local(AdjArgs a) {
     const unsigned s = active ? (unsigned)s0 : 0u;
     const unsigned N = a.N;
     const int x = (int)(s % a.nx), y = (int)((s / a.nx) % a.ny), z = (int)(s / ((unsigned)a.nx * a.ny));
-    const float* mac = a.st + 30 * (size_t)N;
+    const float* mac = a.mac;
     const float dphi = mac[s], u1 = mac[N + s], u2 = mac[2 * N + s], u3 = mac[3 * N + s];
     const float phi = a.phi1 + dphi;
     float v[Q];
@@ -136,17 +140,14 @@ __global__ void __launch_bounds__(256) adj_local(AdjArgs a) {
     const float dA = (p0 - p0ref) - a.kf * phi * lap - a.kf6 * gsq;
     float lphi = 0.f, lA = 0.f, lp = 0.f, lusq = 0.f, lgsq = 0.f;
     float lu[3] = {0.f, 0.f, 0.f}, lgr[3] = {0.f, 0.f, 0.f};
-    double dkf = 0.0, dkg = 0.0, domf = 0.0;
+    // per-site sums in FP32 (15 terms); FP64 from the block sums on (GB300's FP64 rate is low)
+    float dkf = 0.f, dkg = 0.f, domf = 0.f;
     const float wf = a.stream ? a.omf : 1.f, wg = a.stream ? a.omg : 1.f;
 #pragma unroll
     for (int i = 0; i < Q; ++i) {
         const unsigned src = a.stream ? nbr(a, x, y, z, cx(i), cy(i), cz(i)) : s;
         const float ai = a.lin[(size_t)i * N + src];
         const float bi = a.lin[(size_t)(Q + i) * N + src];
-        if (active) {
-            a.lout[(size_t)i * N + s] = (1.f - wf) * ai;
-            a.lout[(size_t)(Q + i) * N + s] = (1.f - wg) * bi;
-        }
         const float Lf = wf * ai, Lg = wg * bi;
         const float cu = cx(i) * u1 + cy(i) * u2 + cz(i) * u3;
         const float cg = cx(i) * gr[0] + cy(i) * gr[1] + cz(i) * gr[2];
@@ -154,7 +155,7 @@ __global__ void __launch_bounds__(256) adj_local(AdjArgs a) {
         const float E = EW(i);
         if (a.stream) {
             const float dfeq = HW(i) * dphi + FW(i) * dA + E * (3.f * phi * cu + a.kf * cGc);
-            domf += (double)ai * (double)(dfeq - a.st[(size_t)i * N + s]);
+            domf += ai * (dfeq - a.st[(size_t)i * N + s]);
         }
         lphi += Lf * (HW(i) + 3.f * E * cu);
         lA += Lf * FW(i);
@@ -162,8 +163,8 @@ __global__ void __launch_bounds__(256) adj_local(AdjArgs a) {
         const float lcGc = Lf * E * a.kf + Lg * E * a.kg;
         lp += Lg * 3.f * E;
         lusq -= 1.5f * Lg * E;
-        dkf += (double)(Lf * E * cGc);
-        dkg += (double)(Lg * E * cGc);
+        dkf += Lf * E * cGc;
+        dkg += Lg * E * cGc;
         lu[0] += lcu * cx(i);
         lu[1] += lcu * cy(i);
         lu[2] += lcu * cz(i);
@@ -176,7 +177,7 @@ __global__ void __launch_bounds__(256) adj_local(AdjArgs a) {
     lu[0] += 2.f * u1 * lusq;
     lu[1] += 2.f * u2 * lusq;
     lu[2] += 2.f * u3 * lusq;
-    dkf += (double)(lA * (-phi * lap - gsq / 6.f));
+    dkf += lA * (-phi * lap - gsq / 6.f);
     lphi += lA * (dp0 - a.kf * lap);
     const float llap = -a.kf * phi * lA;
     lgsq -= a.kf6 * lA;
@@ -194,14 +195,15 @@ __global__ void __launch_bounds__(256) adj_local(AdjArgs a) {
         a.aux[7 * N + s] = lu[1];
         a.aux[8 * N + s] = lu[2];
     } else {
-        dkf = dkg = domf = 0.0;
+        dkf = dkg = domf = 0.f;
     }
-    double gv[3] = {dkf, dkg, domf};
-    block_add<3>(gv, a.grads);
+    double gv[3] = {(double)dkf, (double)dkg, (double)domf};
+    block_add<3>(gv, a.grads + 4 * (blockIdx.x % ADJ_NREP));
 }
 
 // lphi(x) = lphi_loc(x) - 14 llap(x)/5 + sum_k [llap(x - c_k)/5 + c_k . lgrad(x - c_k)/10],
-// then the moments; writes lout (and lphi into phi_out for the initial state)
+// then the moments, plus the streamed (1 - w) part gathered from lin; writes
+// lout (and lphi into phi_out for the initial state)
 __global__ void __launch_bounds__(256) adj_stencil(AdjArgs a, float* phi_out) {
     const long long s0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (s0 >= (long long)a.N) return;
@@ -217,10 +219,15 @@ __global__ void __launch_bounds__(256) adj_stencil(AdjArgs a, float* phi_out) {
     const float lp = a.aux[5 * N + s] * (1.f / 3.f);
     const float lu1 = a.aux[6 * N + s], lu2 = a.aux[7 * N + s], lu3 = a.aux[8 * N + s];
     if (phi_out) phi_out[s] = lphi;
+    // the streamed part (1 - w) of the collision, gathered here rather than
+    // stored by adj_local and read back
+    const float wf = a.stream ? a.omf : 1.f, wg = a.stream ? a.omg : 1.f;
 #pragma unroll
     for (int i = 0; i < Q; ++i) {
-        a.lout[(size_t)i * N + s] += lphi;
-        a.lout[(size_t)(Q + i) * N + s] += lp + (cx(i) * lu1 + cy(i) * lu2 + cz(i) * lu3);
+        const unsigned src = a.stream ? nbr(a, x, y, z, cx(i), cy(i), cz(i)) : s;
+        a.lout[(size_t)i * N + s] = (1.f - wf) * a.lin[(size_t)i * N + src] + lphi;
+        a.lout[(size_t)(Q + i) * N + s] =
+            (1.f - wg) * a.lin[(size_t)(Q + i) * N + src] + (lp + (cx(i) * lu1 + cy(i) * lu2 + cz(i) * lu3));
     }
 }
 
@@ -273,7 +280,7 @@ int adjoint_check(dl_handle* h) {
     if (!h->adj_lam[0]) {
         for (int k = 0; k < 2; ++k) DL_CUDA(h, cudaMalloc(&h->adj_lam[k], sizeof(float) * 30 * h->N));
         DL_CUDA(h, cudaMalloc(&h->adj_aux, sizeof(float) * 9 * h->N));
-        DL_CUDA(h, cudaMalloc(&h->adj_grads, sizeof(double) * 4));
+        DL_CUDA(h, cudaMalloc(&h->adj_grads, sizeof(double) * 4 * ADJ_NREP));
     }
     return DL_OK;
 }
@@ -294,7 +301,7 @@ static inline unsigned nb(long long n) { return (unsigned)((n + 255) / 256); }
 int adjoint_begin(dl_handle* h, const float* d_lphi) {
     int rc = adjoint_check(h);
     if (rc != DL_OK) return rc;
-    DL_CUDA(h, cudaMemsetAsync(h->adj_grads, 0, sizeof(double) * 4, h->stream));
+    DL_CUDA(h, cudaMemsetAsync(h->adj_grads, 0, sizeof(double) * 4 * ADJ_NREP, h->stream));
     h->adj_cur = 0;
     DL_LAUNCH(h, false, (adj_seed<<<nb(h->N), 256, 0, h->stream>>>(d_lphi, h->adj_lam[0], (unsigned)h->N)));
     DL_CUDA(h, cudaGetLastError());
@@ -306,7 +313,8 @@ int adjoint_step(dl_handle* h, const float* d_state, long long step) {
     if (rc != DL_OK) return rc;
     AdjArgs a;
     fill_adj(h, a);
-    a.st = d_state;
+    a.st = d_state;                           // adjoint state: f[15N], fields[5N]
+    a.mac = d_state + (size_t)Q * h->N;
     a.lin = h->adj_lam[h->adj_cur];
     a.lout = h->adj_lam[1 - h->adj_cur];
     a.stream = 1;
@@ -333,7 +341,8 @@ int adjoint_init(dl_handle* h, const float* d_state0, float* d_lphi0) {
     if (rc != DL_OK) return rc;
     AdjArgs a;
     fill_adj(h, a);
-    a.st = d_state0;
+    a.st = d_state0;                          // full state: f[15N], g[15N], fields[5N]
+    a.mac = d_state0 + (size_t)30 * h->N;
     a.lin = h->adj_lam[h->adj_cur];
     a.lout = h->adj_lam[1 - h->adj_cur];
     a.stream = 0;
@@ -346,8 +355,14 @@ int adjoint_init(dl_handle* h, const float* d_state0, float* d_lphi0) {
 
 int adjoint_grads(dl_handle* h, double* out4) {
     if (!h->adj_grads) return set_error(h, DL_ERR_STATE, "no adjoint pass has run");
-    DL_CUDA(h, cudaMemcpyAsync(out4, h->adj_grads, sizeof(double) * 4, cudaMemcpyDeviceToHost, h->stream));
+    double rep[4 * ADJ_NREP];
+    DL_CUDA(h, cudaMemcpyAsync(rep, h->adj_grads, sizeof(rep), cudaMemcpyDeviceToHost, h->stream));
     DL_CUDA(h, cudaStreamSynchronize(h->stream));
+    for (int k = 0; k < 4; ++k) {
+        double s = 0.0;
+        for (int r = 0; r < ADJ_NREP; ++r) s += rep[4 * r + k];
+        out4[k] = s;
+    }
     // d/dtau_f = d/domega_f * d omega_f / d tau_f = -d/domega_f / tau_f^2
     out4[2] = -out4[2] / (h->P.tauf * h->P.tauf);
     return DL_OK;

@@ -279,6 +279,26 @@ int dl_load_state(dl_handle* h, const void* d_src) {
     return DL_OK;
 }
 
+int dl_adjoint_state_floats(dl_handle* h, int64_t* n) {
+    if (!h || !n) return DL_ERR_ARG;
+    if (h->form != DL_FORM_FP32 || h->single)
+        return set_error(h, DL_ERR_UNSUPPORTED, "device state export is for the two-phase FP32 form");
+    *n = (int64_t)20 * (int64_t)h->N;
+    return DL_OK;
+}
+
+int dl_save_adjoint_state(dl_handle* h, void* d_dst) {
+    if (!h || !d_dst) return DL_ERR_ARG;
+    if (h->form != DL_FORM_FP32 || h->single)
+        return set_error(h, DL_ERR_UNSUPPORTED, "device state export is for the two-phase FP32 form");
+    const size_t N = h->N;
+    float* d = (float*)d_dst;
+    DL_CUDA(h, cudaMemcpyAsync(d, h->fs[h->cur], sizeof(float) * Q * N, cudaMemcpyDeviceToDevice, h->stream));
+    DL_CUDA(h, cudaMemcpyAsync(d + Q * N, h->mac32[h->cur], sizeof(float) * 5 * N, cudaMemcpyDeviceToDevice,
+                               h->stream));
+    return DL_OK;
+}
+
 int dl_adjoint_begin(dl_handle* h, const float* d_dloss_dphi) {
     if (!h || !d_dloss_dphi) return DL_ERR_ARG;
     return adjoint_begin(h, d_dloss_dphi);

@@ -275,7 +275,8 @@ int dl_label_droplets(dl_handle* h, int connectivity, int32_t* labels, int64_t* 
  * and walk them backwards with dl_adjoint_step. It covers the shear-droplet
  * physics (walls, static force, viscosity ratio 1, no LES / spectral force). */
 
-/* Number of FP32 values of one device state (populations and fields). */
+/* Number of FP32 values of one full device state (populations and fields;
+ * dl_save_state / dl_load_state / dl_adjoint_init). */
 int dl_state_floats(dl_handle* h, int64_t* n);
 
 /* Copy the current state to / from caller-owned device memory. */
@@ -285,8 +286,14 @@ int dl_load_state(dl_handle* h, const void* d_src);
 /* Start the reverse pass from dLoss/dphi of the final fields (device, N floats). */
 int dl_adjoint_begin(dl_handle* h, const float* d_dloss_dphi);
 
-/* Reverse of time step `step` (1-based); d_state_before is the state saved
- * before that step. */
+/* The part of a state that the reverse of one step reads (f and the fields,
+ * dl_adjoint_state_floats FP32 values): what the recomputed segment keeps per
+ * step, written by dl_save_adjoint_state. */
+int dl_adjoint_state_floats(dl_handle* h, int64_t* n);
+int dl_save_adjoint_state(dl_handle* h, void* d_dst);
+
+/* Reverse of time step `step` (1-based); d_state_before is the adjoint state
+ * (dl_save_adjoint_state) taken before that step. */
 int dl_adjoint_step(dl_handle* h, const void* d_state_before, int64_t step);
 
 /* Reverse of dl_init_equilibrium from the initial state: writes dLoss/dphi0. */
