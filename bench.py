@@ -155,7 +155,7 @@ def phi_error(w, steps: int, stream_ptr: int):
     import numpy as np
     from droplet_gb300.solver import Droplet
 
-    out = {}
+    out, diag = {}, {}
     for form in (64, w.form):
         d = Droplet(w.params, w.shape, form, single_phase=w.single_phase)
         d.set_stream(stream_ptr)
@@ -164,6 +164,7 @@ def phi_error(w, steps: int, stream_ptr: int):
         d.set_force(w.force_mode)
         d.step(steps)
         out[form] = d.get_fields()
+        diag[form] = d.reduce()
         d.close()
     a, b = out[w.form], out[64]
     span = w.params.phi2 - w.params.phi1
@@ -172,6 +173,8 @@ def phi_error(w, steps: int, stream_ptr: int):
            "p_max": float(np.abs(a["p"] - b["p"]).max())}
     if not w.single_phase:
         res["phi_tilde_max"] = float(2.0 * np.abs(a["phi"] - b["phi"]).max() / span)
+        v64 = diag[64]["vol_smooth"]
+        res["volume_drift_rel"] = float((diag[w.form]["vol_smooth"] - v64) / v64)
     return res
 
 
