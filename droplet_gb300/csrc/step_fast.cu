@@ -341,9 +341,10 @@ __device__ __forceinline__ void prefetch_l2(const void* p, unsigned bytes) {
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
-// shared-memory footprint (floats) of the fused kernel
-__host__ __device__ constexpr int fused_smem_floats(bool les, bool spec, bool force) {
-    return NSLOT * P2 * (les ? 4 : 1) + NSLOT * P1 * (12 + (force ? 2 : 0)) +
+// shared-memory footprint (floats) of the fused kernel; the single-phase step
+// stages nothing and keeps records q0, q2 (and q3)
+__host__ __device__ constexpr int fused_smem_floats(bool les, bool spec, bool force, bool sp = false) {
+    return (sp ? 0 : NSLOT * P2 * (les ? 4 : 1)) + NSLOT * P1 * ((sp ? 8 : 12) + (force ? 2 : 0)) +
            (spec ? 2 * (2 * 3 * SNK * EY1) + 2 * (SNK * EX1 + SNK * EY1) + 2 * (3 * 3 * SNK * EY1) : 0);
 }
 
@@ -381,10 +382,10 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
     constexpr bool FORCE = FMODE != F_NONE;
     constexpr bool SPEC = FMODE == F_SPECTRAL;
     constexpr int NSTG = LES ? 4 : 1;                    // staged fields: phi (+ u1, u2, u3)
-    float* s_stg = smem;                                 // [NSLOT][NSTG][P2]
-    float4* s_q0 = (float4*)(s_stg + NSLOT * NSTG * P2); // [NSLOT][P1]
-    float4* s_q1 = s_q0 + NSLOT * P1;
-    float4* s_q2 = s_q1 + NSLOT * P1;
+    float* s_stg = smem;                                 // [NSLOT][NSTG][P2] (none for SP)
+    float4* s_q0 = (float4*)(s_stg + (SP ? 0 : NSLOT * NSTG * P2));  // [NSLOT][P1]
+    float4* s_q1 = s_q0 + NSLOT * P1;                    // (not used by SP)
+    float4* s_q2 = s_q1 + (SP ? 0 : NSLOT * P1);
     float2* s_q3 = (float2*)(s_q2 + NSLOT * P1);         // [NSLOT][P1] (FORCE)
     float2* s_C = s_q3 + (FORCE ? NSLOT * P1 : 0);       // [2][3][SNK][EY1] (SPEC)
     float2* s_tx = s_C + 2 * 3 * SNK * EY1;              // [SNK][EX1] e^{i kx x}
@@ -776,6 +777,14 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
                                      (double)a.phi2, bad, a.step, nblk);
 }
 
+// the single-phase step: a third of the two-phase shared memory, three blocks per SM
+template <typename ST, bool RES, int FMODE>
+__global__ void __launch_bounds__(NT, 3) step_fused_sp(const FastArgs a) {
+    extern __shared__ float smem[];
+    fused_body<ST, RES, false, FMODE, true>(a, smem, blockIdx.x, blockIdx.y, blockIdx.z,
+                                            gridDim.x * gridDim.y * gridDim.z);
+}
+
 template <typename ST, bool RES, bool LES, int FMODE, bool SP = false>
 __global__ void __launch_bounds__(NT, 2) step_fused(const FastArgs a) {
     extern __shared__ float smem[];
@@ -1071,9 +1080,9 @@ __global__ void sp_fhat_from_uh(const double* __restrict__ uh, int K, const int4
 }
 
 // ---- host side ---------------------------------------------------------------------
-template <bool RES, bool LES, int FMODE>
+template <bool RES, bool LES, int FMODE, bool SP = false>
 static size_t smem_bytes() {
-    return sizeof(float) * (size_t)fused_smem_floats(LES, FMODE == F_SPECTRAL, FMODE != F_NONE);
+    return sizeof(float) * (size_t)fused_smem_floats(LES, FMODE == F_SPECTRAL, FMODE != F_NONE, SP);
 }
 
 static void fill_fast(dl_handle* h, FastArgs& a) {
@@ -1308,14 +1317,19 @@ template <typename ST, bool RES, bool LES, int FMODE, bool SP = false>
 static int launch_fused(dl_handle* h, const FastArgs& a) {
     static bool configured[64] = {false};
     const int dev = h->device & 63;
-    const size_t sm = smem_bytes<RES, LES, FMODE>();
+    const size_t sm = smem_bytes<RES, LES, FMODE, SP>();
     if (!configured[dev]) {
-        DL_CUDA(h, cudaFuncSetAttribute(step_fused<ST, RES, LES, FMODE, SP>,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        if constexpr (SP)
+            DL_CUDA(h, cudaFuncSetAttribute(step_fused_sp<ST, RES, FMODE>,
+                                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        else
+            DL_CUDA(h, cudaFuncSetAttribute(step_fused<ST, RES, LES, FMODE>,
+                                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
         configured[dev] = true;
     }
     dim3 grid((a.nx + TX - 1) / TX, (a.ny + TY - 1) / TY, (a.nz + a.lz - 1) / a.lz);
-    DL_LAUNCH(h, true, (step_fused<ST, RES, LES, FMODE, SP><<<grid, NT, sm, h->stream>>>(a)));
+    if constexpr (SP) DL_LAUNCH(h, true, (step_fused_sp<ST, RES, FMODE><<<grid, NT, sm, h->stream>>>(a)));
+    else DL_LAUNCH(h, true, (step_fused<ST, RES, LES, FMODE><<<grid, NT, sm, h->stream>>>(a)));
     DL_CUDA(h, cudaGetLastError());
     if (FMODE == F_SPECTRAL) return launch_projection(h, a);
     return DL_OK;
