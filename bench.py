@@ -326,6 +326,11 @@ def run_ours(args):
                 "kernel": MAIN_KERNEL[form], "kernel_ms": round(avg_main_ms, 5),
                 "kernel_share": round(prof["main_ms"] / max(prof["total_ms"], 1e-12), 4),
                 "algorithmic_bytes_per_launch": bytes_per_launch}
+    if form != 64:
+        # the same pull pattern with no arithmetic, on this GPU, after the timed region
+        ceil_gbps = sim.pull_ceiling(20)
+        roofline["pull_pattern_ceiling"] = round(ceil_gbps, 1)
+        roofline["achieved_over_pull_pattern_ceiling"] = round(achieved / ceil_gbps, 4)
 
     # ---- e2e through the C-ABI with host buffers ------------------------------------
     e2e = None

@@ -47,6 +47,7 @@ SOURCES = {
     "step_fast.cu": FAST,
     "adjoint.cu": FAST,
     "labels.cu": FAST,
+    "ceiling.cu": FAST,
 }
 
 

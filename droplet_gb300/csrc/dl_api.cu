@@ -562,6 +562,11 @@ int dl_energy(dl_handle* h, dl_energy_diag* out, double* spectrum, int64_t nbins
     return energy_diagnostics(h, out, spectrum, (long long)nbins);
 }
 
+int dl_pull_ceiling(dl_handle* h, int repeats, double* gbps) {
+    if (!h || !gbps) return DL_ERR_ARG;
+    return pull_ceiling(h, repeats, gbps);
+}
+
 int dl_reduce(dl_handle* h, dl_diag* out) {
     if (!h || !out) return DL_ERR_ARG;
     int rc = is_fast(h) ? reduce_fields_f32(h, h->mac32[h->cur], out) : reduce_fields(h, h->mac64[h->cur], out);

@@ -214,6 +214,13 @@ class Droplet(_HandleAPI):
         out["spectrum"] = spec[:nb].copy()
         return out
 
+    def pull_ceiling(self, repeats: int = 20) -> float:
+        """GB/s of the step's pull pattern without arithmetic (dl_pull_ceiling);
+        overwrites the next-step population buffer."""
+        v = C.c_double()
+        self._call("pull_ceiling", int(repeats), C.byref(v))
+        return float(v.value)
+
     def reduce_static(self, nblocks: int = 0) -> dict:
         """The diagnostics of reduce() through dl_reduce_static, which
         allocates no device memory (fixed scratch inside the library, shared

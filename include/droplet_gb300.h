@@ -212,6 +212,14 @@ int dl_reduce(dl_handle* h, dl_diag* out);
  * first call plans the transform and allocates its buffers. */
 int dl_energy(dl_handle* h, dl_energy_diag* out, double* spectrum, int64_t nbins);
 
+/* The memory ceiling of the step's access pattern on this GPU, in GB/s: a
+ * z-marching 32 x 8 column kernel pulls the 15 direction arrays of g from
+ * x - c_i and writes them back with no collision, `repeats` times on the
+ * handle's own g buffers (the next-step buffer is overwritten). FP32 and FP16
+ * forms. No counterpart in the reference: it places the fused step's
+ * achieved bandwidth between this ceiling and the copy peak. */
+int dl_pull_ceiling(dl_handle* h, int repeats, double* gbytes_per_s);
+
 /* dl_reduce_static: the same diagnostics as dl_reduce, for callers that must
  * not allocate device memory once their run is set up -- a host program that
  * has reserved nearly all of the GPU's memory for its lattices, or a
