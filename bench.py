@@ -119,6 +119,23 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def max_over_ranks(value: float, dist=None, device: str = "cuda") -> float:
+    """The slowest rank's time: every rank of a replicas run processes its
+    own domain, so the whole job takes as long as its slowest member."""
+    if dist is None:
+        return value
+    import torch
+
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replicas_value(sites_per_rank: int, steps: int, world: int, seconds: float) -> float:
+    """Whole-job MLUPS of N independent replicas (weak scaling)."""
+    return sites_per_rank * steps * world / seconds / 1e6
+
+
 def make_workload(name: str, form: int):
     from droplet_gb300 import configs
 
@@ -309,10 +326,7 @@ def run_ours(args):
     sim.profile(False)
     clk = clocks.stop()
     sim.sync()  # raises if the NaN watchdog tripped
-    if dist is not None:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, dist)
     value = N * args.steps * world / (ms / 1e3) / 1e6
 
     # roofline of the dominant kernel (live per-launch events over the timed region)
@@ -362,10 +376,7 @@ def run_ours(args):
         sim2.get_fields_into(out)
         torch.cuda.synchronize()
         dt = time.perf_counter() - t0
-        if dist is not None:
-            t = torch.tensor([dt], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            dt = float(t.item())
+        dt = max_over_ranks(dt, dist)
         sim2.close()
         from droplet_gb300 import _abi
         import ctypes
