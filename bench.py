@@ -357,8 +357,9 @@ def run_ours(args):
         sim2 = Droplet(w.params, w.shape, w.form, single_phase=w.single_phase)
         sim2.set_stream(stream.cuda_stream)
         if tune is not None:
-            sim2.set_option("lz", tune["lz"])
-            sim2.set_option("prefetch", tune["prefetch"])
+            for k in ("lz", "prefetch", "pipeline"):
+                if k in tune:
+                    sim2.set_option(k, tune[k])
         torch.cuda.synchronize()
         if dist is not None:
             dist.barrier()

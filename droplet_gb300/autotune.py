@@ -11,6 +11,7 @@ timing. The cache lives at $DROPLET_GB300_TUNE_CACHE or
 """
 from __future__ import annotations
 
+import itertools
 import json
 import os
 import threading
@@ -71,32 +72,38 @@ def _key(kind: str, form: int, shapes, extra: str) -> str:
 
 
 def tune_droplet(sim, steps: int = 20, use_cache: bool = True) -> dict:
-    """Pick "lz" and "prefetch" for one Droplet (fast forms). Returns the
-    chosen settings."""
+    """Pick "lz" and "prefetch" (and, for the single-phase step, "pipeline")
+    for one Droplet (fast forms). Returns the chosen settings."""
     p = sim.params
+    single = bool(getattr(sim, "single_phase", False))
     key = _key("single", sim.form, [(sim.nx, sim.ny, sim.nz)],
-               f"les{int(bool(p.les))}" + ("_1phase" if getattr(sim, "single_phase", False) else "") + "_pf")
+               f"les{int(bool(p.les))}" + ("_1phase" if single else "") + "_pf")
+    knobs = ["prefetch"] + (["pipeline"] if single else [])
     if use_cache:
         hit = _load().get(key)
         if hit:
             sim.set_option("lz", hit["lz"])
-            sim.set_option("prefetch", hit["prefetch"])
+            for k in knobs:
+                sim.set_option(k, hit[k])
             return dict(hit, cached=True)
     best = None
     timings = {}
-    for pf in (0, 1):
-        sim.set_option("prefetch", pf)
+    combos = [dict(zip(knobs, v)) for v in itertools.product((0, 1), repeat=len(knobs))]
+    for combo in combos:
+        for k, v in combo.items():
+            sim.set_option(k, v)
         for lz in LZ_CANDIDATES:
             if lz > sim.nz:
                 continue
             sim.set_option("lz", lz)
             ms = _time_steps(sim, steps)
-            timings[f"lz{lz}_pf{pf}"] = ms
+            timings["lz%d_" % lz + "_".join(f"{k}{v}" for k, v in combo.items())] = ms
             if best is None or ms < best[2]:
-                best = (lz, pf, ms)
+                best = (lz, combo, ms)
     sim.set_option("lz", best[0])
-    sim.set_option("prefetch", best[1])
-    res = {"lz": best[0], "prefetch": best[1], "ms_per_step": best[2], "timings": timings}
+    for k, v in best[1].items():
+        sim.set_option(k, v)
+    res = dict({"lz": best[0], "ms_per_step": best[2], "timings": timings}, **best[1])
     _store(key, res)
     return dict(res, cached=False)
 

@@ -331,6 +331,11 @@ int dl_set_option(dl_handle* h, const char* key, int64_t value) {
         h->l2_prefetch = (int)value;
         return DL_OK;
     }
+    if (strcmp(key, "pipeline") == 0) {
+        if (value < 0 || value > 1) return set_error(h, DL_ERR_ARG, "pipeline must be 0 or 1");
+        h->sp_pipeline = (int)value;
+        return DL_OK;
+    }
     return set_error(h, DL_ERR_ARG, "unknown option '%s'", key);
 }
 
@@ -342,6 +347,10 @@ int dl_get_option(dl_handle* h, const char* key, int64_t* value) {
     }
     if (strcmp(key, "prefetch") == 0) {
         *value = h->l2_prefetch;
+        return DL_OK;
+    }
+    if (strcmp(key, "pipeline") == 0) {
+        *value = h->sp_pipeline;
         return DL_OK;
     }
     return set_error(h, DL_ERR_ARG, "unknown option '%s'", key);

@@ -137,6 +137,7 @@ struct dl_handle {
     float* force32;          // [3][N]
     int lz;                  // z planes per block of the fused kernel
     int l2_prefetch;         // fused kernel: bulk L2 prefetch of the next plane's pulls
+    int sp_pipeline;         // single-phase kernel: next plane's pulls held in registers
     // dl_energy: cuFFT plan and buffers (allocated on first use)
     long long en_plan;
     int en_plan_ok;

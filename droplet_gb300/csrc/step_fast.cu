@@ -376,8 +376,10 @@ __device__ __forceinline__ RecPos rec_pos(int tid, int j) {
     return r;
 }
 
-// SP: the single-phase step (g only; no staging, no phi stencils)
-template <typename ST, bool RES, bool LES, int FMODE, bool SP = false>
+// SP: the single-phase step (g only; no staging, no phi stencils).
+// PIPE (SP only): the next plane's pulls are issued before this plane's
+// collision, so two planes of loads are in flight per thread.
+template <typename ST, bool RES, bool LES, int FMODE, bool SP = false, bool PIPE = false>
 __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int bx, int by, int bz, unsigned nblk) {
     constexpr bool FORCE = FMODE != F_NONE;
     constexpr bool SPEC = FMODE == F_SPECTRAL;
@@ -645,6 +647,19 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
     float bmin = INFINITY, bmax = -INFINITY;
     bool bad = false;
 
+    // g pulled from x - c_i at plane zp (the PIPE register stage)
+    auto pull_g = [&](int zp, float* v) {
+        unsigned zq[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) zq[d] = (unsigned)wrap_near(zp - 1 + d, nz) * nxy;
+#pragma unroll
+        for (int i = 0; i < Q; ++i) v[i] = Pop<ST>::ld(a.g, (unsigned)i * N + zq[1 - cz(i)] + yr[1 - cy(i)] + xs[1 - cx(i)]);
+    };
+    float gnx[Q];
+    if constexpr (PIPE) {
+        if (act) pull_g(z0, gnx);
+    }
+
     for (int z = z0; z < z1; ++z) {
         float2 tz1, tz2;  // twiddles of plane z+2 (their latency hides behind the pulls)
         if (SPEC) ztw(z + 2, tz1, tz2);
@@ -653,7 +668,10 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
 #pragma unroll
         for (int d = 0; d < 3; ++d) zo[d] = (unsigned)wrap_near(z - 1 + d, nz) * nxy;
         float fin[Q], gin[Q];
-        if (act) {
+        if constexpr (PIPE) {
+#pragma unroll
+            for (int i = 0; i < Q; ++i) gin[i] = gnx[i];
+        } else if (act) {
 #pragma unroll
             for (int i = 0; i < Q; ++i) {
                 const unsigned src = zo[1 - cz(i)] + yr[1 - cy(i)] + xs[1 - cx(i)];
@@ -665,6 +683,9 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
         cp_async_wait_all();  // plane z+3
         __syncthreads();
         if (z + 4 <= z1 + 1) stage(z + 4);  // slot of plane z, last read by records(z+1)
+        if constexpr (PIPE) {
+            if (act && z + 1 < z1) pull_g(z + 1, gnx);
+        }
         if (a.l2_prefetch && z + 1 < z1) pull_prefetch(z + 1);
         if (z + 2 <= z1) records(z + 2);
         if (z + 3 <= z1) prefetch(z + 3);
@@ -783,6 +804,14 @@ __global__ void __launch_bounds__(NT, 3) step_fused_sp(const FastArgs a) {
     extern __shared__ float smem[];
     fused_body<ST, RES, false, FMODE, true>(a, smem, blockIdx.x, blockIdx.y, blockIdx.z,
                                             gridDim.x * gridDim.y * gridDim.z);
+}
+
+// the same with the next plane's pulls in registers: two blocks per SM
+template <typename ST, bool RES, int FMODE>
+__global__ void __launch_bounds__(NT, 2) step_fused_sp_pipe(const FastArgs a) {
+    extern __shared__ float smem[];
+    fused_body<ST, RES, false, FMODE, true, true>(a, smem, blockIdx.x, blockIdx.y, blockIdx.z,
+                                                  gridDim.x * gridDim.y * gridDim.z);
 }
 
 template <typename ST, bool RES, bool LES, int FMODE, bool SP = false>
@@ -1316,20 +1345,31 @@ static int launch_projection(dl_handle* h, const FastArgs& a) {
 template <typename ST, bool RES, bool LES, int FMODE, bool SP = false>
 static int launch_fused(dl_handle* h, const FastArgs& a) {
     static bool configured[64] = {false};
+    static bool configured_pipe[64] = {false};
     const int dev = h->device & 63;
     const size_t sm = smem_bytes<RES, LES, FMODE, SP>();
-    if (!configured[dev]) {
-        if constexpr (SP)
-            DL_CUDA(h, cudaFuncSetAttribute(step_fused_sp<ST, RES, FMODE>,
-                                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        else
+    const bool pipe = SP && h->sp_pipeline;
+    if (!(pipe ? configured_pipe[dev] : configured[dev])) {
+        if constexpr (SP) {
+            if (pipe)
+                DL_CUDA(h, cudaFuncSetAttribute(step_fused_sp_pipe<ST, RES, FMODE>,
+                                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+            else
+                DL_CUDA(h, cudaFuncSetAttribute(step_fused_sp<ST, RES, FMODE>,
+                                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        } else {
             DL_CUDA(h, cudaFuncSetAttribute(step_fused<ST, RES, LES, FMODE>,
                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        configured[dev] = true;
+        }
+        (pipe ? configured_pipe[dev] : configured[dev]) = true;
     }
     dim3 grid((a.nx + TX - 1) / TX, (a.ny + TY - 1) / TY, (a.nz + a.lz - 1) / a.lz);
-    if constexpr (SP) DL_LAUNCH(h, true, (step_fused_sp<ST, RES, FMODE><<<grid, NT, sm, h->stream>>>(a)));
-    else DL_LAUNCH(h, true, (step_fused<ST, RES, LES, FMODE><<<grid, NT, sm, h->stream>>>(a)));
+    if constexpr (SP) {
+        if (pipe) DL_LAUNCH(h, true, (step_fused_sp_pipe<ST, RES, FMODE><<<grid, NT, sm, h->stream>>>(a)));
+        else DL_LAUNCH(h, true, (step_fused_sp<ST, RES, FMODE><<<grid, NT, sm, h->stream>>>(a)));
+    } else {
+        DL_LAUNCH(h, true, (step_fused<ST, RES, LES, FMODE><<<grid, NT, sm, h->stream>>>(a)));
+    }
     DL_CUDA(h, cudaGetLastError());
     if (FMODE == F_SPECTRAL) return launch_projection(h, a);
     return DL_OK;

@@ -47,9 +47,11 @@ def start(sim, f, mode, force):
         sim.set_force(mode)
 
 
-def run(kind, form, shape, steps):
+def run(kind, form, shape, steps, pipeline=0):
     P, f, mode, force = case(kind, shape)
     g = Droplet(P, shape, form, single_phase=True)
+    if form != FORM_FP64:
+        g.set_option("pipeline", pipeline)
     o = pyoracle.OracleDroplet(P, shape)
     start(g, f, mode, force)
     start(o, f, mode, force)
@@ -75,13 +77,14 @@ def test_fp64_single_phase_bitwise(kind):
         assert not fa.any()
 
 
+@pytest.mark.parametrize("pipeline", [0, 1])
 @pytest.mark.parametrize("form,tol_u,tol_p", [(FORM_FP32, 2e-6, 2e-6), (FORM_FP16, 1e-4, 1e-4)])
 @pytest.mark.parametrize("kind", ["plain", "static_force", "spectral", "walls"])
-def test_fast_single_phase_tracks_oracle(form, tol_u, tol_p, kind):
-    """40 x 20 x 16 (x not a multiple of the 32-wide tile), 30 steps;
-    absolute tolerances on u and p."""
+def test_fast_single_phase_tracks_oracle(form, tol_u, tol_p, kind, pipeline):
+    """40 x 20 x 16 (x not a multiple of the 32-wide tile), 30 steps, both
+    kernel variants; absolute tolerances on u and p."""
     shape = (40, 20, 16)
-    P, g, o = run(kind, form, shape, 30)
+    P, g, o = run(kind, form, shape, 30, pipeline)
     a, b = g.get_fields(), o.get_fields()
     eu = max(np.abs(a[k] - b[k]).max() for k in ("u1", "u2", "u3"))
     ep = np.abs(a["p"] - b["p"]).max()
