@@ -146,7 +146,7 @@ __device__ __forceinline__ float csumf(const float* v) {
 __device__ __forceinline__ float site_dp0(const FastArgs& a, float dphi) {
     const float phi = __fadd_rn(a.phi1, dphi);
     const float den = __fmul_rn(__fmaf_rn(-a.b, phi, 1.f), a.omb1);
-    const float t = __fdiv_rn(a.T, den);
+    const float t = __fmul_rn(a.T, __frcp_rn(den));  // reciprocal, not a full division
     return __fmul_rn(dphi, __fmaf_rn(-a.a, __fadd_rn(phi, a.phi1), t));
 }
 
@@ -189,7 +189,7 @@ struct Rec {
 // v[1..14]: dphi at the D3Q15 neighbours; w[c][1..14]: u_c there (LES only)
 template <bool LES>
 __device__ __forceinline__ Rec make_record(const FastArgs& a, float dphi, const float* v, const float (*w)[Q],
-                                           float u1, float u2, float u3, float dp, float mn, float mx) {
+                                           float u1, float u2, float u3, float dp, float mn, float kscale) {
     Rec r;
     float lap = -14.f * dphi;
 #pragma unroll
@@ -207,7 +207,7 @@ __device__ __forceinline__ Rec make_record(const FastArgs& a, float dphi, const 
     r.u2 = u2;
     r.u3 = u3;
     r.S = site_S(dp, u1, u2, u3);
-    const float nu = (phi - mn) / (mx - mn) * a.dnu + a.nu1;
+    const float nu = (phi - mn) * kscale + a.nu1;  // kscale = dnu / (phi_max - phi_min), per block
     float nut = 0.f;
     if (LES) {
         float gu[9];
@@ -222,9 +222,10 @@ __device__ __forceinline__ Rec make_record(const FastArgs& a, float dphi, const 
         const float sxz = 0.5f * (gu[0 + 3 * 2] + gu[2 + 3 * 0]);
         const float syz = 0.5f * (gu[1 + 3 * 2] + gu[2 + 3 * 1]);
         const float ss = gu[0] * gu[0] + gu[4] * gu[4] + gu[8] * gu[8] + 2.f * (sxy * sxy + sxz * sxz + syz * syz);
-        nut = a.csd * sqrtf(2.f * ss);
+        const float t = 2.f * ss;
+        nut = t > 0.f ? a.csd * (t * rsqrtf(t)) : 0.f;
     }
-    r.omg = 1.f / (0.5f + 3.f * (nu + nut) * a.inv_ds + a.anu23);
+    r.omg = __frcp_rn(0.5f + 3.f * (nu + nut) * a.inv_ds + a.anu23);
     r.Fx = r.Fy = r.Fz = 0.f;
     return r;
 }
@@ -408,6 +409,7 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
         mn = (float)a.st->phi_min;
         mx = (float)a.st->phi_max;
     }
+    const float kscale = a.dnu / (mx - mn);  // nu = (phi - mn) kscale + nu1
     // ---- per-thread wrapped offsets (computed once) ----
     unsigned soff[2];  // staging positions k = tid, tid + NT (P2 = 432 < 2 NT)
 #pragma unroll
@@ -575,7 +577,7 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
                 u2 = pf_u[j][1];
                 u3 = pf_u[j][2];
             }
-            const Rec r = make_record<LES>(a, stc[c2], v, w, u1, u2, u3, pf_dp[j], mn, mx);
+            const Rec r = make_record<LES>(a, stc[c2], v, w, u1, u2, u3, pf_dp[j], mn, kscale);
             s_q0[o] = make_float4(r.dphi, r.u1, r.u2, r.u3);
             s_q1[o] = make_float4(r.gx, r.gy, r.gz, r.dA);
             s_q2[o] = make_float4(r.S, r.omg, RES ? r.dp0 : 1.5f * r.gsq, F[0]);
@@ -957,7 +959,7 @@ __global__ void __launch_bounds__(256) init_fast(const FastArgs a) {
         v[i] = a.mac[nb];
     }
     const float u1 = a.mac[N + s], u2 = a.mac[2 * N + s], u3 = a.mac[3 * N + s], dp = a.mac[4 * N + s];
-    const Rec r = make_record<false>(a, a.mac[s], v, nullptr, u1, u2, u3, dp, a.phi1, a.phi2);
+    const Rec r = make_record<false>(a, a.mac[s], v, nullptr, u1, u2, u3, dp, a.phi1, a.dnu / (a.phi2 - a.phi1));
     const float phi = __fadd_rn(a.phi1, r.dphi);
 #pragma unroll
     for (int i = 0; i < Q; ++i) {
