@@ -345,6 +345,20 @@ def run_ours(args):
         ceil_gbps = sim.pull_ceiling(20)
         roofline["pull_pattern_ceiling"] = round(ceil_gbps, 1)
         roofline["achieved_over_pull_pattern_ceiling"] = round(achieved / ceil_gbps, 4)
+    else:
+        # the plain form is bound by the FP64 pipe: flops from the committed SASS counts,
+        # peak = this GPU's measured FP64 FMA throughput
+        flops = committed_traffic(f"flops:{MAIN_KERNEL[form]}_{args.form}", w.name)
+        peak64 = sim.fp64_ceiling()
+        hbm = dict(roofline)
+        roofline = {"bound": "fp64", "achieved": None, "peak": round(peak64, 4), "unit": "TFLOP/s", "frac": None,
+                    "traffic": None, "peak_source": "measured (dl_fp64_ceiling)", "kernel": MAIN_KERNEL[form],
+                    "kernel_ms": hbm["kernel_ms"], "kernel_share": hbm["kernel_share"],
+                    "flops_per_launch": flops, "hbm": hbm}
+        if flops:
+            tf = flops / (avg_main_ms / 1e3) / 1e12
+            roofline["achieved"] = round(tf, 4)
+            roofline["frac"] = round(tf / peak64, 4)
 
     # ---- e2e through the C-ABI with host buffers ------------------------------------
     e2e = None

@@ -154,6 +154,8 @@ def declare(lib: C.CDLL, prefix: str) -> None:
         lib.dl_set_stream.restype = C.c_int
         lib.dl_reduce.argtypes = [h, C.POINTER(DLDiag)]
         lib.dl_reduce.restype = C.c_int
+        lib.dl_fp64_ceiling.argtypes = [h, C.POINTER(C.c_double)]
+        lib.dl_fp64_ceiling.restype = C.c_int
         lib.dl_pull_ceiling.argtypes = [h, C.c_int, C.POINTER(C.c_double)]
         lib.dl_pull_ceiling.restype = C.c_int
         lib.dl_energy.argtypes = [h, C.POINTER(DLEnergyDiag), C.c_void_p, C.c_int64]
@@ -238,6 +240,7 @@ HEADER_SYMBOLS = [
     "dl_reduce_static",
     "dl_energy",
     "dl_pull_ceiling",
+    "dl_fp64_ceiling",
     "dl_sync",
     "dl_last_error",
     "dl_profile",

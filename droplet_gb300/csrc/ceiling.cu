@@ -1,10 +1,13 @@
-// ceiling.cu -- dl_pull_ceiling: the memory ceiling of the step's access
+// ceiling.cu -- measured ceilings beside the roofline.
+// dl_pull_ceiling: the memory ceiling of the step's access
 // pattern on this GPU. A z-marching 32 x 8 column kernel pulls the 15
 // direction arrays of g from x - c_i (periodic) and writes them to the other
 // buffer, with no collision: what the fused step's loads and stores cost
 // without its arithmetic. It runs on the handle's own g buffers (the
 // next-step buffer is overwritten, the current one is only read) and is
 // timed with CUDA events on the handle's stream.
+// dl_fp64_ceiling: FP64 FMA throughput of this GPU (the bound of the plain
+// FP64 form), from independent FMA chains on every SM.
 #include "dl_internal.cuh"
 
 #include <cuda_fp16.h>
@@ -63,6 +66,46 @@ int pull_ceiling(dl_handle* h, int repeats, double* gbps) {
     DL_CUDA(h, cudaGetLastError());
     const double bytes = 2.0 * Q * (half ? 2.0 : 4.0) * (double)h->N;
     *gbps = bytes / ((double)ms / repeats * 1e-3) / 1e9;
+    return DL_OK;
+}
+
+// FP64 FMA throughput: 8 independent chains per thread, 4 blocks per SM
+__global__ void __launch_bounds__(256) fma64_loop(double* out, int iters, double a, double b) {
+    double v[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) v[k] = (double)(threadIdx.x + k) * 1e-3;
+    for (int it = 0; it < iters; ++it)
+#pragma unroll
+        for (int k = 0; k < 8; ++k) v[k] = fma(v[k], a, b);
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) s += v[k];
+    if (out && s == 12345.6789) out[0] = s;  // keeps the chains live (out is null)
+}
+
+int fp64_ceiling(dl_handle* h, double* tflops) {
+    int sms = 0;
+    DL_CUDA(h, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device));
+    const int blocks = 4 * sms, iters = 4096;
+    double* sink = nullptr;
+    fma64_loop<<<blocks, 256, 0, h->stream>>>(sink, iters, 0.999999, 1e-7);  // warm-up
+    cudaEvent_t e0, e1;
+    DL_CUDA(h, cudaEventCreate(&e0));
+    DL_CUDA(h, cudaEventCreate(&e1));
+    cudaEventRecord(e0, h->stream);
+    const int reps = 5;
+    for (int r = 0; r < reps; ++r) fma64_loop<<<blocks, 256, 0, h->stream>>>(sink, iters, 0.999999, 1e-7);
+    cudaEventRecord(e1, h->stream);
+    cudaError_t e = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    DL_CUDA(h, e);
+    DL_CUDA(h, cudaGetLastError());
+    h->launches += reps + 1;
+    const double flops = 2.0 * 8.0 * iters * 256.0 * blocks * reps;
+    *tflops = flops / ((double)ms * 1e-3) / 1e12;
     return DL_OK;
 }
 

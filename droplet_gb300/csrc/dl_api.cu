@@ -576,6 +576,11 @@ int dl_pull_ceiling(dl_handle* h, int repeats, double* gbps) {
     return pull_ceiling(h, repeats, gbps);
 }
 
+int dl_fp64_ceiling(dl_handle* h, double* tflops) {
+    if (!h || !tflops) return DL_ERR_ARG;
+    return fp64_ceiling(h, tflops);
+}
+
 int dl_reduce(dl_handle* h, dl_diag* out) {
     if (!h || !out) return DL_ERR_ARG;
     int rc = is_fast(h) ? reduce_fields_f32(h, h->mac32[h->cur], out) : reduce_fields(h, h->mac64[h->cur], out);

@@ -215,6 +215,7 @@ int fill_doubles(dl_handle* h, double* d, double v, size_t n);
 int energy_diagnostics(dl_handle* h, dl_energy_diag* out, double* spectrum_host, long long nbins);
 void energy_free(dl_handle* h);
 int pull_ceiling(dl_handle* h, int repeats, double* gbps);
+int fp64_ceiling(dl_handle* h, double* tflops);
 // diagnostics (reduce.cu)
 int reduce_fields(dl_handle* h, const double* d_mac, dl_diag* out);
 int reduce_fields_f32(dl_handle* h, const float* d_mac, dl_diag* out);

@@ -221,6 +221,12 @@ class Droplet(_HandleAPI):
         self._call("pull_ceiling", int(repeats), C.byref(v))
         return float(v.value)
 
+    def fp64_ceiling(self) -> float:
+        """Measured FP64 FMA throughput of this GPU, TFLOP/s (dl_fp64_ceiling)."""
+        v = C.c_double()
+        self._call("fp64_ceiling", C.byref(v))
+        return float(v.value)
+
     def reduce_static(self, nblocks: int = 0) -> dict:
         """The diagnostics of reduce() through dl_reduce_static, which
         allocates no device memory (fixed scratch inside the library, shared

@@ -220,6 +220,10 @@ int dl_energy(dl_handle* h, dl_energy_diag* out, double* spectrum, int64_t nbins
  * achieved bandwidth between this ceiling and the copy peak. */
 int dl_pull_ceiling(dl_handle* h, int repeats, double* gbytes_per_s);
 
+/* FP64 FMA throughput of this GPU in TFLOP/s (2 flops per FMA), the bound of
+ * the plain FP64 form; runs on the handle's stream. No reference counterpart. */
+int dl_fp64_ceiling(dl_handle* h, double* tflops);
+
 /* dl_reduce_static: the same diagnostics as dl_reduce, for callers that must
  * not allocate device memory once their run is set up -- a host program that
  * has reserved nearly all of the GPU's memory for its lattices, or a
