@@ -425,7 +425,9 @@ int dl_set_force(dl_handle* h, int mode, const double* fx, const double* fy, con
     const size_t N = h->N;
     if (mode != DL_FORCE_NONE && mode != DL_FORCE_STATIC && mode != DL_FORCE_SPECTRAL) return DL_ERR_ARG;
     if (mode == DL_FORCE_SPECTRAL && (h->P.kc < 2 || h->sp.K < 1))
-        return set_error(h, DL_ERR_ARG, "spectral forcing needs kc >= 2");
+        return set_error(h, DL_ERR_ARG,
+                         "spectral forcing needs kc >= 2 and a domain holding the band (2 kc - 1 <= nx, ny; "
+                         "kc <= nz / 2)");
     if (is_fast(h)) {
         int rc = fast_prepare_force(h, mode);
         if (rc != DL_OK) return rc;

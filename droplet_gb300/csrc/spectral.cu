@@ -314,8 +314,11 @@ int spectral_alloc(dl_handle* h) {
     const int K = h->P.kc - 1;
     sp.K = K;
     if (K < 1) return DL_OK;
-    if (2 * K + 1 > h->nx || 2 * K + 1 > h->ny || K + 1 > h->nz / 2)
-        return set_error(h, DL_ERR_ARG, "domain too small for kc=%d", h->P.kc);
+    if (2 * K + 1 > h->nx || 2 * K + 1 > h->ny || K + 1 > h->nz / 2) {
+        // no band plan: dl_set_force(DL_FORCE_SPECTRAL) refuses; the step itself works
+        sp.K = 0;
+        return DL_OK;
+    }
     const int NK = 2 * K + 1;
     int rc;
     if ((rc = upload_twiddle(h, h->nx, &sp.d_twx)) != DL_OK) return rc;

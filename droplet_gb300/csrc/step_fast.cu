@@ -1172,6 +1172,7 @@ static int fast_spectral_alloc(dl_handle* h) {
     memset(&fs, 0, sizeof(fs));
     const int K = h->P.kc - 1;
     if (K < 1 || K > SK) return DL_OK;  // kc > 3: separate forcing launches
+    if (2 * K + 1 > h->nx || 2 * K + 1 > h->ny || K + 1 > h->nz / 2) return DL_OK;  // band does not fit
     std::vector<int4> modes;
     std::vector<int> off(SNK + 1, 0);
     for (int kx = -SK; kx <= SK; ++kx) {
