@@ -281,11 +281,14 @@ __device__ void spectral_finalize(const FastArgs& a) {
     const int nv = 6 * a.nm;  // values per accumulator copy
     // fold the copies into copy 0 (fixed order)
     for (int t = tid; t < nv; t += blockDim.x) {
-        double v = __ldcg(a.acc + t);
-        for (int r = 1; r < SP_NREP; ++r) {
-            v += __ldcg(a.acc + (size_t)r * nv + t);
-            a.acc[(size_t)r * nv + t] = 0.0;
-        }
+        double c[SP_NREP];  // all loads first, so that they are in flight together
+#pragma unroll
+        for (int r = 0; r < SP_NREP; ++r) c[r] = __ldcg(a.acc + (size_t)r * nv + t);
+        double v = c[0];
+#pragma unroll
+        for (int r = 1; r < SP_NREP; ++r) v += c[r];
+#pragma unroll
+        for (int r = 1; r < SP_NREP; ++r) a.acc[(size_t)r * nv + t] = 0.0;
         a.acc[t] = v;
     }
     __syncthreads();
