@@ -4,7 +4,7 @@
 //    program/turbulence_hit_xy.f90:588-645: u_hat = FFT(u)/N (fft_r2c,
 //    :725-730), summed over the reference's index set k1 in [0,nx),
 //    k2 in [0,ny), k3 in [0,nz/2] with weight 1 on k3 = 0 and 2 elsewhere,
-//    into bin int(|k|) + 1 with the signed wavenumbers of judge (:739-746);
+//    into bin int(|k|) + 1 with the signed wavenumbers of the function judge (:739-746);
 //    the FFTs are cuFFT D2Z transforms in FP64, modes outside the stored half
 //    are read through Hermitian symmetry;
 //  * sums of the bulk free energy psi = phi T ln(phi/(1 - b phi)) - a phi^2

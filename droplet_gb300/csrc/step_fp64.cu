@@ -15,7 +15,7 @@
 //                 moments (physics :541-552) and reduce phi min/max
 //                 (:559-574) with one atomic per block; the last block turns
 //                 the reduction into the next step's tau_g range.
-// On GB300 this form is bound by the FP64 pipe, not by HBM; see the design doc.
+// On GB300 this form is bound by the FP64 pipe, not by HBM (about 1.7k FP64 flops per site).
 #include "dl_internal.cuh"
 #include "dl_device.cuh"
 

@@ -2,7 +2,7 @@
 dl_energy). TEST INFRASTRUCTURE ONLY.
 
 * spectrum: enesupe_cal, program/turbulence_hit_xy.f90:588-645, with
-  u_hat = FFT(u)/N (fft_r2c, :725-730) and the signed wavenumbers of judge
+  u_hat = FFT(u)/N (fft_r2c, :725-730) and the signed wavenumbers of the function judge
   (:739-746): over k1 in [0,nx), k2 in [0,ny), k3 in [0,nz/2],
   E[int(|k|)] += 0.5 (|u1_hat|^2 + |u2_hat|^2 + |u3_hat|^2) (1 if k3 == 0 else 2).
 * free energy: free_energy_cal (program/energy_budget.f90:1012-1023) and
