@@ -160,6 +160,8 @@ def declare(lib: C.CDLL, prefix: str) -> None:
         lib.dl_pull_ceiling.restype = C.c_int
         lib.dl_energy.argtypes = [h, C.POINTER(DLEnergyDiag), C.c_void_p, C.c_int64]
         lib.dl_energy.restype = C.c_int
+        lib.dl_get_minmax_async.argtypes = [h, _vp]
+        lib.dl_get_minmax_async.restype = C.c_int
         lib.dl_reduce_static.argtypes = [h, C.c_int, C.POINTER(DLDiag)]
         lib.dl_reduce_static.restype = C.c_int
         lib.dl_sync.argtypes = [h]
@@ -236,6 +238,7 @@ HEADER_SYMBOLS = [
     "dl_set_step",
     "dl_get_step",
     "dl_get_minmax",
+    "dl_get_minmax_async",
     "dl_reduce",
     "dl_reduce_static",
     "dl_energy",

@@ -558,6 +558,13 @@ int dl_get_minmax(dl_handle* h, double* mn, double* mx) {
     return DL_OK;
 }
 
+int dl_get_minmax_async(dl_handle* h, double* dst) {
+    if (!h || !dst) return DL_ERR_ARG;
+    // phi_min and phi_max are the first two fields of the device state
+    DL_CUDA(h, cudaMemcpyAsync(dst, h->d_state, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    return DL_OK;
+}
+
 int dl_sync(dl_handle* h) {
     if (!h) return DL_ERR_ARG;
     DL_CUDA(h, cudaStreamSynchronize(h->stream));

@@ -170,6 +170,11 @@ class _HandleAPI:
         self._call("get_minmax", C.byref(mn), C.byref(mx))
         return float(mn.value), float(mx.value)
 
+    def minmax_async(self, pinned_ptr: int):
+        """Enqueue the copy of (phi_min, phi_max) into two pinned host doubles
+        at pinned_ptr; read them once the stream has passed this point."""
+        self._call("get_minmax_async", C.c_void_p(int(pinned_ptr)))
+
 
 class Droplet(_HandleAPI):
     """Whole-domain droplet state resident on the current CUDA device."""

@@ -197,6 +197,14 @@ int dl_get_step(dl_handle* h, int64_t* step);
  * phi_min/phi_max after the MPI_Allreduce, program/lbm_drop_xy.f90:559-574. */
 int dl_get_minmax(dl_handle* h, double* phi_min, double* phi_max);
 
+/* The same two values without waiting: enqueues their copy into
+ * dst[0] = phi_min, dst[1] = phi_max on the handle's stream and returns. dst
+ * must be page-locked host memory (cudaHostAlloc / pinned) that stays valid
+ * until the copy is done; read it after the stream (or an event recorded
+ * after this call) has completed. Lets a host read every step's result one
+ * step behind while the GPU keeps stepping. */
+int dl_get_minmax_async(dl_handle* h, double* dst);
+
 /* FP64 diagnostics of the current fields; replaces the ad-hoc sums of the
  * analysis programs (kinetic.d in program/lbm_iht_xy.f90:777-822, the
  * droplet moments of prototype_program/two-phase/drop8_mpi.f90:812-970). */

@@ -155,3 +155,21 @@ def test_fast_form_profile_counts_launches():
     g.step(7)
     s = g.profile_read()
     assert s["main_launches"] == 7 and s["launches"] == 7 and s["main_ms"] > 0
+
+
+@pytest.mark.parametrize("form", [FORM_FP64, FORM_FP32])
+def test_minmax_async_equals_minmax(form):
+    """dl_get_minmax_async copies into pinned memory the same two values that
+    dl_get_minmax returns once the stream has passed the copy."""
+    import torch
+
+    shape = (24, 20, 16)
+    P, f, mode, force = make_case("plain", shape)
+    g = Droplet(P, shape, form)
+    start(g, f, mode, force)
+    buf = torch.zeros(2, dtype=torch.float64).pin_memory()
+    for _ in range(3):
+        g.step(1)
+        g.minmax_async(buf.data_ptr())
+        g.sync()
+        assert (float(buf[0]), float(buf[1])) == g.minmax()
