@@ -180,6 +180,21 @@ struct Pop<__half> {
     static __device__ __forceinline__ void st(void* p, long long i, float v) { ((__half*)p)[i] = __float2half_rn(v); }
 };
 
+// ---- packed FP32x2 stencil sums (two staged fields per 64-bit word) -------------
+// sum_{i=1..14} c_{AL,i} v[i] for both lanes: FADD2 for +1, FFMA2 with -1 for -1
+template <int AL>
+__device__ __forceinline__ float2 csum2(const float2* v) {
+    float2 s = make_float2(0.f, 0.f);
+    const float2 m1 = make_float2(-1.f, -1.f);
+#pragma unroll
+    for (int i = 1; i < Q; ++i) {
+        const int c = AL == 0 ? cx(i) : (AL == 1 ? cy(i) : cz(i));
+        if (c == 1) s = __fadd2_rn(s, v[i]);
+        else if (c == -1) s = __ffma2_rn(v[i], m1, s);
+    }
+    return s;
+}
+
 // ---- the per-site record ------------------------------------------------------
 struct Rec {
     float dphi, u1, u2, u3, dA, S, omg, gx, gy, gz, gsq, dp0, Fx, Fy, Fz;
@@ -225,6 +240,52 @@ __device__ __forceinline__ Rec make_record(const FastArgs& a, float dphi, const 
         const float t = 2.f * ss;
         nut = t > 0.f ? a.csd * (t * rsqrtf(t)) : 0.f;
     }
+    r.omg = __frcp_rn(0.5f + 3.f * (nu + nut) * a.inv_ds + a.anu23);
+    r.Fx = r.Fy = r.Fz = 0.f;
+    return r;
+}
+
+// the LES record from pairs (phi - phi1, u1) and (u2, u3) at the 14 neighbours:
+// the same sums as make_record<true>, two fields per packed instruction
+__device__ __forceinline__ Rec make_record_les2(const FastArgs& a, float dphi, const float2* pa, const float2* pb,
+                                                float u1, float u2, float u3, float dp, float mn, float kscale) {
+    Rec r;
+    float lap = -14.f * dphi;
+#pragma unroll
+    for (int i = 1; i < Q; ++i) lap += pa[i].x;
+    lap *= a.inv_lap;
+    const float2 ax = csum2<0>(pa), ay = csum2<1>(pa), az = csum2<2>(pa);  // (d phi, d u1)
+    const float2 bx = csum2<0>(pb), by = csum2<1>(pb), bz = csum2<2>(pb);  // (d u2, d u3)
+    r.gx = ax.x * a.inv_grad;
+    r.gy = ay.x * a.inv_grad;
+    r.gz = az.x * a.inv_grad;
+    r.gsq = r.gx * r.gx + r.gy * r.gy + r.gz * r.gz;
+    const float phi = __fadd_rn(a.phi1, dphi);
+    r.dp0 = site_dp0(a, dphi);
+    r.dA = r.dp0 - a.kf * phi * lap - a.kf6 * r.gsq;
+    r.dphi = dphi;
+    r.u1 = u1;
+    r.u2 = u2;
+    r.u3 = u3;
+    r.S = site_S(dp, u1, u2, u3);
+    const float nu = (phi - mn) * kscale + a.nu1;
+    // gu[c + 3 al] = d u_c / d x_al
+    float gu[9];
+    gu[0] = ax.y * a.inv_grad;
+    gu[3] = ay.y * a.inv_grad;
+    gu[6] = az.y * a.inv_grad;
+    gu[1] = bx.x * a.inv_grad;
+    gu[4] = by.x * a.inv_grad;
+    gu[7] = bz.x * a.inv_grad;
+    gu[2] = bx.y * a.inv_grad;
+    gu[5] = by.y * a.inv_grad;
+    gu[8] = bz.y * a.inv_grad;
+    const float sxy = 0.5f * (gu[0 + 3 * 1] + gu[1 + 3 * 0]);
+    const float sxz = 0.5f * (gu[0 + 3 * 2] + gu[2 + 3 * 0]);
+    const float syz = 0.5f * (gu[1 + 3 * 2] + gu[2 + 3 * 1]);
+    const float ss = gu[0] * gu[0] + gu[4] * gu[4] + gu[8] * gu[8] + 2.f * (sxy * sxy + sxz * sxz + syz * syz);
+    const float t = 2.f * ss;
+    const float nut = t > 0.f ? a.csd * (t * rsqrtf(t)) : 0.f;
     r.omg = __frcp_rn(0.5f + 3.f * (nu + nut) * a.inv_ds + a.anu23);
     r.Fx = r.Fy = r.Fz = 0.f;
     return r;
@@ -472,12 +533,14 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
             const int k = tid + j * NT;
             if (k >= P2) continue;
             const unsigned s = zo + soff[j];
-            float* dst = s_stg + slot * NSTG * P2 + k;
-            cp_async4(dst, a.mac + s);
-            if (LES) {
-                cp_async4(dst + P2, a.mac + N + s);
+            if (LES) {  // pairs (phi - phi1, u1) then (u2, u3)
+                float* dst = s_stg + slot * NSTG * P2 + 2 * k;
+                cp_async4(dst, a.mac + s);
+                cp_async4(dst + 1, a.mac + N + s);
                 cp_async4(dst + 2 * P2, a.mac + 2 * N + s);
-                cp_async4(dst + 3 * P2, a.mac + 3 * N + s);
+                cp_async4(dst + 2 * P2 + 1, a.mac + 3 * N + s);
+            } else {
+                cp_async4(s_stg + slot * NSTG * P2 + k, a.mac + s);
             }
         }
         cp_async_commit();
@@ -556,31 +619,29 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
                 continue;
             }
             const int c2 = (rp.ey + 1) * EX2 + (rp.ex + 1);
-            float v[Q];
+            Rec r;
+            if constexpr (LES) {
+                float2 pa[Q], pb[Q];
 #pragma unroll
-            for (int i = 1; i < Q; ++i) {
-                const float* st = cz(i) == 0 ? stc : (cz(i) > 0 ? stp : stm);
-                v[i] = st[c2 + cy(i) * EX2 + cx(i)];
-            }
-            float u1, u2, u3;
-            float w[3][Q];
-            if (LES) {
-                u1 = stc[P2 + c2];
-                u2 = stc[2 * P2 + c2];
-                u3 = stc[3 * P2 + c2];
-#pragma unroll
-                for (int c = 0; c < 3; ++c)
-#pragma unroll
-                    for (int i = 1; i < Q; ++i) {
-                        const float* st = cz(i) == 0 ? stc : (cz(i) > 0 ? stp : stm);
-                        w[c][i] = st[(1 + c) * P2 + c2 + cy(i) * EX2 + cx(i)];
-                    }
+                for (int i = 1; i < Q; ++i) {
+                    const float* st = cz(i) == 0 ? stc : (cz(i) > 0 ? stp : stm);
+                    const int q = c2 + cy(i) * EX2 + cx(i);
+                    pa[i] = reinterpret_cast<const float2*>(st)[q];
+                    pb[i] = reinterpret_cast<const float2*>(st + 2 * P2)[q];
+                }
+                const float2 ca = reinterpret_cast<const float2*>(stc)[c2];
+                const float2 cb = reinterpret_cast<const float2*>(stc + 2 * P2)[c2];
+                r = make_record_les2(a, ca.x, pa, pb, ca.y, cb.x, cb.y, pf_dp[j], mn, kscale);
             } else {
-                u1 = pf_u[j][0];
-                u2 = pf_u[j][1];
-                u3 = pf_u[j][2];
+                float v[Q];
+#pragma unroll
+                for (int i = 1; i < Q; ++i) {
+                    const float* st = cz(i) == 0 ? stc : (cz(i) > 0 ? stp : stm);
+                    v[i] = st[c2 + cy(i) * EX2 + cx(i)];
+                }
+                r = make_record<false>(a, stc[c2], v, nullptr, pf_u[j][0], pf_u[j][1], pf_u[j][2], pf_dp[j], mn,
+                                       kscale);
             }
-            const Rec r = make_record<LES>(a, stc[c2], v, w, u1, u2, u3, pf_dp[j], mn, kscale);
             s_q0[o] = make_float4(r.dphi, r.u1, r.u2, r.u3);
             s_q1[o] = make_float4(r.gx, r.gy, r.gz, r.dA);
             s_q2[o] = make_float4(r.S, r.omg, RES ? r.dp0 : 1.5f * r.gsq, F[0]);
