@@ -455,7 +455,7 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
     float4* s_q2 = s_q1 + (SP ? 0 : NSLOT * P1);
     float2* s_q3 = (float2*)(s_q2 + NSLOT * P1);         // [NSLOT][P1] (FORCE)
     float2* s_C = s_q3 + (FORCE ? NSLOT * P1 : 0);       // [2][3][SNK][EY1] (SPEC)
-    float2* s_tx = s_C + 2 * 3 * SNK * EY1;              // [SNK][EX1] e^{i kx x}
+    float2* s_tx = s_C + 2 * 3 * SNK * EY1;              // [SNK][EX1] (cos kx x, -sin kx x)
     float2* s_ty = s_tx + SNK * EX1;                     // [SNK][EY1] e^{i ky y}
     float2* s_D = s_ty + SNK * EY1;                      // [3][SNK][EY1][3] z-free part of C, by kz
     const int tid = threadIdx.x;
@@ -499,7 +499,8 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
     if (SPEC) {
         for (int t = tid; t < SNK * EX1; t += NT) {
             const int kxi = t / EX1, ex = t % EX1;
-            s_tx[t] = a.twx[pmod((kxi - SK) * pmod(x0 - 1 + ex, nx), nx)];
+            const float2 e = a.twx[pmod((kxi - SK) * pmod(x0 - 1 + ex, nx), nx)];
+            s_tx[t] = make_float2(e.x, -e.y);  // Re(C e^{i kx x}) = C . (cos, -sin)
         }
         for (int t = tid; t < SNK * EY1; t += NT) {
             const int kyi = t / EY1, ey = t % EY1;
@@ -600,15 +601,16 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
                 F[1] = __ldg(a.force + N + s);
                 F[2] = __ldg(a.force + 2 * N + s);
             } else if (SPEC) {
+                // F_c = sum_kx Re(C e^{i kx x}): one FFMA2 per term, the two lanes added at the end
+                float2 acc[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
 #pragma unroll
                 for (int kxi = 0; kxi < SNK; ++kxi) {
                     const float2 e = s_tx[kxi * EX1 + rp.ex];
 #pragma unroll
-                    for (int c = 0; c < 3; ++c) {
-                        const float2 cv = C[(c * SNK + kxi) * EY1 + rp.ey];
-                        F[c] += cv.x * e.x - cv.y * e.y;
-                    }
+                    for (int c = 0; c < 3; ++c) acc[c] = __ffma2_rn(C[(c * SNK + kxi) * EY1 + rp.ey], e, acc[c]);
                 }
+#pragma unroll
+                for (int c = 0; c < 3; ++c) F[c] = acc[c].x + acc[c].y;
             }
             const int o = sc * P1 + rp.k;
             if constexpr (SP) {
