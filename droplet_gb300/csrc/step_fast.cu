@@ -334,13 +334,17 @@ __device__ __forceinline__ float collide_g(int i, float S, float omg, float u1, 
 }
 
 // last block: band energy E = sum_m 0.5 w_m |u_hat_m|^2, u_hat = acc / N, and
-// the coefficients w_m (0.5 eps / E) u_hat_m of the next step; zeroes acc
+// the coefficients w_m (0.5 eps / E) u_hat_m of the next step; zeroes acc.
+// The folded sums stay in shared memory, so the block reads acc once.
 __device__ void spectral_finalize(const FastArgs& a) {
     __shared__ double s_e[NWARP];
     __shared__ double s_coef;
+    __shared__ double s_acc[6 * SMAXM];
+    __shared__ double s_w[SMAXM];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nv = 6 * a.nm;  // values per accumulator copy
-    // fold the copies into copy 0 (fixed order)
+    if (tid < a.nm) s_w[tid] = (double)__ldg(a.modes + tid).w;
+    // fold the copies (fixed order), zero them
     for (int t = tid; t < nv; t += blockDim.x) {
         double c[SP_NREP];  // all loads first, so that they are in flight together
 #pragma unroll
@@ -349,8 +353,8 @@ __device__ void spectral_finalize(const FastArgs& a) {
 #pragma unroll
         for (int r = 1; r < SP_NREP; ++r) v += c[r];
 #pragma unroll
-        for (int r = 1; r < SP_NREP; ++r) a.acc[(size_t)r * nv + t] = 0.0;
-        a.acc[t] = v;
+        for (int r = 0; r < SP_NREP; ++r) a.acc[(size_t)r * nv + t] = 0.0;
+        s_acc[t] = v;
     }
     __syncthreads();
     double e = 0.0;
@@ -358,11 +362,11 @@ __device__ void spectral_finalize(const FastArgs& a) {
         double s = 0.0;
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            const double re = a.acc[2 * (c * a.nm + m)] * a.invN;
-            const double im = a.acc[2 * (c * a.nm + m) + 1] * a.invN;
+            const double re = s_acc[2 * (c * a.nm + m)] * a.invN;
+            const double im = s_acc[2 * (c * a.nm + m) + 1] * a.invN;
             s += re * re + im * im;
         }
-        e += 0.5 * (double)a.modes[m].w * s;
+        e += 0.5 * s_w[m] * s;
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
@@ -379,11 +383,8 @@ __device__ void spectral_finalize(const FastArgs& a) {
     const double coef = s_coef;
     for (int t = tid; t < 3 * a.nm; t += blockDim.x) {
         const int m = t % a.nm;
-        const double k = coef * a.invN * (double)a.modes[m].w;
-        double* p = a.acc + 2 * t;
-        a.fh_next[t] = make_float2((float)(k * p[0]), (float)(k * p[1]));
-        p[0] = 0.0;
-        p[1] = 0.0;
+        const double k = coef * a.invN * s_w[m];
+        a.fh_next[t] = make_float2((float)(k * s_acc[2 * t]), (float)(k * s_acc[2 * t + 1]));
     }
 }
 
@@ -891,84 +892,113 @@ __global__ void __launch_bounds__(NT, 2) step_fused(const FastArgs a) {
 
 // ---- band projection of the new u (F_SPECTRAL) ---------------------------------------
 // acc[c][m] += sum over sites of u_c e^{-i k_m.x}: one warp per (y, z) row,
-// lanes over x with the x twiddles, warp sums, then each lane owns two band
-// modes and applies e^{-i (ky y + kz z)}; block sum and one FP64 atomic per
-// value; the block that finishes last turns acc into the next coefficients.
+// lanes over x with the x twiddles, a transposed warp sum of the row's 15
+// values, then each lane owns two band modes and applies e^{-i (ky y + kz z)};
+// block sum and one FP64 atomic per value; the block that finishes last turns
+// acc into the next coefficients.
 constexpr int PROJ_NT = 256;
+constexpr int SNV = 2 * SK + 1;  // values of a row per component: sum u_c, then Re, Im of k = 1..SK
+constexpr int NRV = 16;          // the 3 SNV values padded to 16 for the lane transpose
+static_assert(3 * SNV <= NRV, "row values exceed the lane transpose");
 
-__device__ void project_rows(const FastArgs& a, long long row0, long long row1, unsigned nblk) {
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+// sum of v[0..15] over the warp, transposed: each exchange halves the values a
+// lane holds; afterwards lanes 2j and 2j+1 hold the total of value j
+__device__ __forceinline__ float warp_transpose_sum16(float (&v)[NRV], int lane) {
+#pragma unroll
+    for (int h = NRV / 2, o = 16; h >= 1; h >>= 1, o >>= 1) {
+        const bool up = (lane & o) != 0;
+#pragma unroll
+        for (int j = 0; j < h; ++j) {
+            const float send = up ? v[j] : v[j + h];
+            const float keep = up ? v[j + h] : v[j];
+            v[j] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+        }
+    }
+    return v[0] + __shfl_xor_sync(0xffffffffu, v[0], 1);
+}
+
+// k y reduced into [0, n) for |k| <= SK
+__device__ __forceinline__ int wrap_k(int ky, int n) {
+#pragma unroll
+    for (int s = 0; s < SK; ++s) {
+        ky = ky < 0 ? ky + n : ky;
+        ky = ky >= n ? ky - n : ky;
+    }
+    return ky;
+}
+
+// rows first, first + stride, ... below nrows, one per warp iteration
+__device__ void project_rows(const FastArgs& a, int first, int stride, int nrows, unsigned nblk) {
+    const int tid = threadIdx.x, lane = tid & 31;
     const int nx = a.nx, ny = a.ny, nz = a.nz;
     const long long N = a.N;
     const float* u[3] = {a.maco + N, a.maco + 2 * N, a.maco + 3 * N};
+    // the lane's two modes (absent modes: k = 0, never accumulated)
+    int kx[2], ky[2], kz[2];
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+        const int m = lane + 32 * j;
+        const int4 md = m < a.nm ? __ldg(a.modes + m) : make_int4(0, 0, 0, 0);
+        kx[j] = md.x;
+        ky[j] = md.y;
+        kz[j] = md.z;
+    }
     float pacc[2][3][2];
 #pragma unroll
     for (int j = 0; j < 2; ++j)
 #pragma unroll
         for (int c = 0; c < 3; ++c) pacc[j][c][0] = pacc[j][c][1] = 0.f;
-    for (long long row = row0 + warp; row < row1; row += PROJ_NT / 32) {
-        const int z = (int)(row / ny), y = (int)(row - (long long)z * ny);
-        const long long base = row * nx;
-        float sr[3][SK + 1], si[3][SK + 1];
+    const int dz = stride / ny, dy = stride - dz * ny;
+    int z = first / ny, y = first - z * ny;
+    for (int row = first; row < nrows; row += stride) {
+        const long long base = (long long)row * nx;
+        float v[NRV];
 #pragma unroll
-        for (int c = 0; c < 3; ++c)
-#pragma unroll
-            for (int k = 0; k <= SK; ++k) sr[c][k] = si[c][k] = 0.f;
+        for (int t = 0; t < NRV; ++t) v[t] = 0.f;
+#pragma unroll 4
         for (int x = lane; x < nx; x += 32) {
             float uv[3];
 #pragma unroll
             for (int c = 0; c < 3; ++c) uv[c] = u[c][base + x];
 #pragma unroll
+            for (int c = 0; c < 3; ++c) v[c * SNV] += uv[c];
+#pragma unroll
             for (int k = 1; k <= SK; ++k) {
                 int ix = k * x;
-                ix = ix >= nx ? ix - nx : ix;
+#pragma unroll
+                for (int s = 1; s < k; ++s) ix = ix >= nx ? ix - nx : ix;
                 const float2 e = a.twx[ix];
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
-                    sr[c][k] += uv[c] * e.x;
-                    si[c][k] -= uv[c] * e.y;
+                    v[c * SNV + 2 * k - 1] = fmaf(uv[c], e.x, v[c * SNV + 2 * k - 1]);
+                    v[c * SNV + 2 * k] = fmaf(-uv[c], e.y, v[c * SNV + 2 * k]);
                 }
             }
-#pragma unroll
-            for (int c = 0; c < 3; ++c) sr[c][0] += uv[c];
         }
-#pragma unroll
-        for (int c = 0; c < 3; ++c)
-#pragma unroll
-            for (int k = 0; k <= SK; ++k)
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) {
-                    sr[c][k] += __shfl_xor_sync(0xffffffffu, sr[c][k], o);
-                    if (k > 0) si[c][k] += __shfl_xor_sync(0xffffffffu, si[c][k], o);
-                }
+        const float tot = warp_transpose_sum16(v, lane);
 #pragma unroll
         for (int j = 0; j < 2; ++j) {
-            const int m = lane + 32 * j;
-            if (m >= a.nm) continue;
-            const int4 md = __ldg(a.modes + m);
-            // (k y) mod n for |k| <= SK: k y lies in (-SK n, SK n)
-            int iy = (md.y * y) % ny;
-            iy = iy < 0 ? iy + ny : iy;
-            const int iz = (md.z * z) % nz;
-            const float2 ey = a.twy[iy], ez = a.twz[iz];
+            const int ak = kx[j] < 0 ? -kx[j] : kx[j];
+            const float2 ey = a.twy[wrap_k(ky[j] * y, ny)], ez = a.twz[wrap_k(kz[j] * z, nz)];
             const float pr = ey.x * ez.x - ey.y * ez.y;
             const float pi = -(ey.x * ez.y + ey.y * ez.x);
-            const int ak = md.x < 0 ? -md.x : md.x;
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
-                float xr = sr[c][0], xi = 0.f;
-#pragma unroll
-                for (int k = 1; k <= SK; ++k)
-                    if (k == ak) {
-                        xr = sr[c][k];
-                        xi = si[c][k];
-                    }
-                if (md.x < 0) xi = -xi;
+                const float xr = __shfl_sync(0xffffffffu, tot, 2 * (c * SNV + (ak ? 2 * ak - 1 : 0)));
+                float xi = __shfl_sync(0xffffffffu, tot, 2 * (c * SNV + 2 * ak));
+                xi = ak ? (kx[j] < 0 ? -xi : xi) : 0.f;
                 pacc[j][c][0] += xr * pr - xi * pi;
                 pacc[j][c][1] += xr * pi + xi * pr;
             }
         }
+        y += dy;
+        z += dz;
+        if (y >= ny) {
+            y -= ny;
+            z += 1;
+        }
     }
+    const int warp = tid >> 5;
     __shared__ float red[PROJ_NT / 32][3][SMAXM][2];
 #pragma unroll
     for (int j = 0; j < 2; ++j) {
@@ -1001,10 +1031,10 @@ __device__ void project_rows(const FastArgs& a, long long row0, long long row1, 
     if (tid == 0) a.st->sp_done = 0u;
 }
 
-__global__ void __launch_bounds__(PROJ_NT) sp_project_fast(const FastArgs a, int rows_per_block) {
-    const long long rows = (long long)a.ny * a.nz;
-    const long long r0 = (long long)blockIdx.x * rows_per_block;
-    project_rows(a, r0, min(r0 + rows_per_block, rows), gridDim.x);
+// rows dealt to the grid's warps in turn, so that every SM gets the same share
+__global__ void __launch_bounds__(PROJ_NT, 4) sp_project_fast(const FastArgs a) {
+    constexpr int W = PROJ_NT / 32;
+    project_rows(a, blockIdx.x * W + (threadIdx.x >> 5), gridDim.x * W, a.ny * a.nz, gridDim.x);
 }
 
 // ---- initial populations f = feq, g = geq at every site (ini :244-251) -------
@@ -1396,17 +1426,16 @@ static int fast_spectral_project(dl_handle* h) {
 
 static const int PROJ_ROWS = 64;  // rows of the band projection per block (batched ensembles)
 
-// band projection launch: three blocks per SM (the register limit), rows
-// split evenly so that no SM runs a second wave alone
+// band projection launch: four blocks on every SM (the register limit), one
+// wave; fewer blocks when there are fewer rows than warps
 static int launch_projection(dl_handle* h, const FastArgs& a) {
     const long long rows = (long long)a.ny * a.nz;
     static int sm_count[64] = {0};
     int& sms = sm_count[h->device & 63];
     if (sms == 0 && cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device) != cudaSuccess) sms = 152;
-    const long long want = 3LL * sms;
-    const int rpb = (int)((rows + want - 1) / want);
-    const unsigned grid = (unsigned)((rows + rpb - 1) / rpb);
-    DL_LAUNCH(h, false, (sp_project_fast<<<grid, PROJ_NT, 0, h->stream>>>(a, rpb)));
+    const long long need = (rows + PROJ_NT / 32 - 1) / (PROJ_NT / 32);
+    const unsigned grid = (unsigned)std::min<long long>(4LL * sms, need);
+    DL_LAUNCH(h, false, (sp_project_fast<<<grid, PROJ_NT, 0, h->stream>>>(a)));
     DL_CUDA(h, cudaGetLastError());
     return DL_OK;
 }
@@ -1564,9 +1593,9 @@ __global__ void __launch_bounds__(PROJ_NT) sp_project_batched(const FastArgs* __
         int* dst = (int*)&s_a;
         for (int t = threadIdx.x; t < (int)(sizeof(FastArgs) / sizeof(int)); t += blockDim.x) dst[t] = src[t];
         __syncthreads();
-        const long long rows = (long long)s_a.ny * s_a.nz;
-        const long long r0 = (long long)it.y * rows_per_item;
-        project_rows(s_a, r0, min(r0 + rows_per_item, rows), nblk_of[it.x]);
+        const int rows = s_a.ny * s_a.nz;
+        const int r0 = it.y * rows_per_item;
+        project_rows(s_a, r0 + (threadIdx.x >> 5), PROJ_NT / 32, min(r0 + rows_per_item, rows), nblk_of[it.x]);
     }
 }
 
