@@ -159,6 +159,9 @@ int dl_create(const dl_params* params, int nx, int ny, int nz, int form, dl_hand
     // L2 prefetch of the next plane's pulled rows: pays off where arithmetic,
     // not bandwidth, sets the pace (the two-phase FP32 step); "prefetch" option
     h->l2_prefetch = (!single && form == DL_FORM_FP32) ? 1 : 0;
+    // band forcing: the new u is projected by each block of the fused step
+    // after its march ("projection" option; 0: a launch of its own)
+    h->proj_in_step = 1;
     if (single) {
         // the precursor step: constant nu1, no interface terms
         h->P.kappaf = 0.0;
@@ -336,6 +339,11 @@ int dl_set_option(dl_handle* h, const char* key, int64_t value) {
         h->sp_pipeline = (int)value;
         return DL_OK;
     }
+    if (strcmp(key, "projection") == 0) {
+        if (value < 0 || value > 1) return set_error(h, DL_ERR_ARG, "projection must be 0 or 1");
+        h->proj_in_step = (int)value;
+        return DL_OK;
+    }
     return set_error(h, DL_ERR_ARG, "unknown option '%s'", key);
 }
 
@@ -351,6 +359,10 @@ int dl_get_option(dl_handle* h, const char* key, int64_t* value) {
     }
     if (strcmp(key, "pipeline") == 0) {
         *value = h->sp_pipeline;
+        return DL_OK;
+    }
+    if (strcmp(key, "projection") == 0) {
+        *value = h->proj_in_step;
         return DL_OK;
     }
     return set_error(h, DL_ERR_ARG, "unknown option '%s'", key);

@@ -138,6 +138,7 @@ struct dl_handle {
     int lz;                  // z planes per block of the fused kernel
     int l2_prefetch;         // fused kernel: bulk L2 prefetch of the next plane's pulls
     int sp_pipeline;         // single-phase kernel: next plane's pulls held in registers
+    int proj_in_step;        // band forcing: projection of the new u inside the fused step (else its own launch)
     // dl_energy: cuFFT plan and buffers (allocated on first use)
     long long en_plan;
     int en_plan_ok;

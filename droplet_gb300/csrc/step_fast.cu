@@ -63,6 +63,7 @@ constexpr int SP_NREP = 16;           // copies of the projection accumulators (
 struct FastArgs {
     int nx, ny, nz, lz;
     int l2_prefetch;
+    int proj_in_step;  // band projection of the new u at the end of the fused step (F_SPECTRAL)
     long long N;
     const float* mac;  // [5][N] dphi, u1, u2, u3, dp
     float* maco;
@@ -333,14 +334,18 @@ __device__ __forceinline__ float collide_g(int i, float S, float omg, float u1, 
     return go;
 }
 
+// shared scratch of spectral_finalize (doubles)
+constexpr int FIN_SCRATCH = 6 * SMAXM + SMAXM + NWARP + 1;
+
 // last block: band energy E = sum_m 0.5 w_m |u_hat_m|^2, u_hat = acc / N, and
 // the coefficients w_m (0.5 eps / E) u_hat_m of the next step; zeroes acc.
-// The folded sums stay in shared memory, so the block reads acc once.
-__device__ void spectral_finalize(const FastArgs& a) {
-    __shared__ double s_e[NWARP];
-    __shared__ double s_coef;
-    __shared__ double s_acc[6 * SMAXM];
-    __shared__ double s_w[SMAXM];
+// The folded sums stay in shared memory (scratch: FIN_SCRATCH doubles), so the
+// block reads acc once.
+__device__ void spectral_finalize(const FastArgs& a, double* scratch) {
+    double* s_acc = scratch;
+    double* s_w = s_acc + 6 * SMAXM;
+    double* s_e = s_w + SMAXM;
+    double& s_coef = s_e[NWARP];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nv = 6 * a.nm;  // values per accumulator copy
     if (tid < a.nm) s_w[tid] = (double)__ldg(a.modes + tid).w;
@@ -388,6 +393,143 @@ __device__ void spectral_finalize(const FastArgs& a) {
     }
 }
 
+// the tile's halo-indexed twiddle tables: s_tx[kx][ex] = (cos kx x, -sin kx x),
+// s_ty[ky][ey] = e^{i ky y}, x = x0 - 1 + ex, y = y0 - 1 + ey
+__device__ __forceinline__ void tile_twiddles(const FastArgs& a, float2* s_tx, float2* s_ty, int x0, int y0) {
+    for (int t = threadIdx.x; t < SNK * EX1; t += NT) {
+        const int kxi = t / EX1, ex = t % EX1;
+        const float2 e = a.twx[pmod((kxi - SK) * pmod(x0 - 1 + ex, a.nx), a.nx)];
+        s_tx[t] = make_float2(e.x, -e.y);  // Re(C e^{i kx x}) = C . (cos, -sin)
+    }
+    for (int t = threadIdx.x; t < SNK * EY1; t += NT) {
+        const int kyi = t / EY1, ey = t % EY1;
+        s_ty[t] = a.twy[pmod((kyi - SK) * pmod(y0 - 1 + ey, a.ny), a.ny)];
+    }
+}
+
+// ---- band projection of the block's own tile, after its z march -----------------
+// acc[c][m] += sum over the tile of u_c e^{-i k_m.x}, factorised: each thread
+// sums its site column over z for kz = 0, 1, 2 (it re-reads the u it wrote);
+// the block sums the columns over x for kx = -2..2 per row, then over y per
+// mode; one FP64 atomic per value; the block that finishes last (of nblk)
+// turns acc into the next coefficients. scr: shared scratch of PT_SCRATCH
+// floats that nothing else uses any more; s_tx (cos kx x, -sin kx x) and s_ty
+// (e^{i ky y}) are the block's halo-indexed twiddle tables.
+constexpr int PT_NV = 15;  // column values: per component sum u, Re/Im sum u e^{-iz}, Re/Im sum u e^{-2iz}
+constexpr int PT_NR = SNK * 3 * 3 * TY;  // row sums (kx, c, kz, row), complex
+constexpr int PT_SCRATCH = PT_NV * NT + 2 * PT_NR + 2 * FIN_SCRATCH;
+static_assert(3 * 3 * 3 * TY <= NT, "one row sum of kx >= 0 per thread");
+
+__device__ __forceinline__ void project_tile(const FastArgs& a, float* scr, const float2* s_tx, const float2* s_ty,
+                                             int gxd, int gyd, int z0, int z1, bool act, unsigned rep) {
+    const int tid = threadIdx.x;
+    const int nx = a.nx, nz = a.nz;
+    const unsigned N = (unsigned)a.N, nxy = (unsigned)a.nx * (unsigned)a.ny;
+    float* sC = scr;                                    // [PT_NV][NT]
+    float2* sR = reinterpret_cast<float2*>(scr + PT_NV * NT);  // [SNK][3][3][TY]
+    float cs[3][5];
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int j = 0; j < 5; ++j) cs[c][j] = 0.f;
+    if (act) {
+        // planes in batches of PB: all of a batch's loads are in flight together
+        constexpr int PB = 8;
+        const unsigned col = (unsigned)gyd * (unsigned)nx + (unsigned)gxd;
+        for (int zb = z0; zb < z1; zb += PB) {
+            float u[PB][3];
+            float2 e1[PB], e2[PB];
+#pragma unroll
+            for (int k = 0; k < PB; ++k) {
+                const int z = zb + k;
+                if (z < z1) {
+                    const unsigned s = (unsigned)z * nxy + col;
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) u[k][c] = a.maco[(unsigned)(c + 1) * N + s];  // written by this thread
+                    int i2 = 2 * z;
+                    i2 = i2 >= nz ? i2 - nz : i2;
+                    e1[k] = __ldg(a.twz + z);
+                    e2[k] = __ldg(a.twz + i2);
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < PB; ++k) {
+                if (zb + k < z1) {
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        cs[c][0] += u[k][c];
+                        cs[c][1] = fmaf(u[k][c], e1[k].x, cs[c][1]);
+                        cs[c][2] = fmaf(-u[k][c], e1[k].y, cs[c][2]);
+                        cs[c][3] = fmaf(u[k][c], e2[k].x, cs[c][3]);
+                        cs[c][4] = fmaf(-u[k][c], e2[k].y, cs[c][4]);
+                    }
+                }
+            }
+        }
+    }
+    __syncthreads();  // every warp is past its last use of the scratch region
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int j = 0; j < 5; ++j) sC[(c * 5 + j) * NT + tid] = cs[c][j];
+    __syncthreads();
+    // row sums over x: thread (kxa, c, kz, row) forms kx = +kxa and -kxa together
+    if (tid < 3 * 3 * 3 * TY) {
+        const int row = tid % TY, kz = (tid / TY) % 3, c = (tid / (3 * TY)) % 3, kxa = tid / (9 * TY);
+        const int vr = c * 5 + (kz == 0 ? 0 : 2 * kz - 1);
+        const float* cr = sC + vr * NT + row * TX;
+        const float* ci = sC + (vr + 1) * NT + row * TX;  // read only for kz > 0
+        const float2* e = s_tx + (kxa + SK) * EX1 + 1;
+        const int lane = tid & 31;
+        float P = 0.f, Qs = 0.f, R = 0.f, S = 0.f;
+#pragma unroll 8
+        for (int i = 0; i < TX; ++i) {
+            const int xx = (i + lane) & (TX - 1);  // rotated: no bank conflicts
+            const float r = cr[xx], im = kz ? ci[xx] : 0.f;
+            const float2 t = e[xx];  // (cos, -sin) of kxa x
+            P = fmaf(r, t.x, P);
+            Qs = fmaf(-im, t.y, Qs);
+            R = fmaf(im, t.x, R);
+            S = fmaf(-r, t.y, S);
+        }
+        // (r + i im) e^{-i kxa x} = (P + Qs) + i (R - S); with e^{+i kxa x}: (P - Qs) + i (R + S)
+        sR[(((kxa + SK) * 3 + c) * 3 + kz) * TY + row] = make_float2(P + Qs, R - S);
+        if (kxa) sR[(((SK - kxa) * 3 + c) * 3 + kz) * TY + row] = make_float2(P - Qs, R + S);
+    }
+    __syncthreads();
+    // per mode and component: sum over rows with e^{-i ky y}, one FP64 atomic each for Re, Im
+    for (int t = tid; t < 3 * a.nm; t += NT) {
+        const int c = t / a.nm, m = t - c * a.nm;
+        const int4 md = __ldg(a.modes + m);
+        const float2* r = sR + (((md.x + SK) * 3 + c) * 3 + md.z) * TY;
+        const float2* ey = s_ty + (md.y + SK) * EY1 + 1;
+        float re = 0.f, im = 0.f;
+#pragma unroll
+        for (int row = 0; row < TY; ++row) {
+            const float2 v = r[row], w = ey[row];  // v e^{-i ky y} = v conj(w)
+            re += v.x * w.x + v.y * w.y;
+            im += v.y * w.x - v.x * w.y;
+        }
+        double* dst = a.acc + (size_t)(rep % SP_NREP) * (6 * a.nm) + 2 * (c * a.nm + m);
+        atomicAdd(dst, (double)re);
+        atomicAdd(dst + 1, (double)im);
+    }
+}
+
+// after all of the block's tiles: the block that finishes last (of nblk) turns
+// acc into the next coefficients (scratch as for project_tile)
+__device__ __forceinline__ void spectral_block_done(const FastArgs& a, float* scr, unsigned nblk) {
+    __threadfence();
+    __shared__ int s_last;
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = (atomicAdd(&a.st->sp_done, 1u) == nblk - 1);
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    spectral_finalize(a, reinterpret_cast<double*>(scr + PT_NV * NT + 2 * PT_NR));
+    if (threadIdx.x == 0) a.st->sp_done = 0u;
+}
+
 // ---- the fused step kernel ---------------------------------------------------
 // Per z plane one barrier: the staging ring and the record ring have four
 // slots; the records of plane z+2 are built in the same barrier interval as
@@ -413,6 +555,8 @@ __host__ __device__ constexpr int fused_smem_floats(bool les, bool spec, bool fo
     return (sp ? 0 : NSLOT * P2 * (les ? 4 : 1)) + NSLOT * P1 * ((sp ? 8 : 12) + (force ? 2 : 0)) +
            (spec ? 2 * (2 * 3 * SNK * EY1) + 2 * (SNK * EX1 + SNK * EY1) + 2 * (3 * 3 * SNK * EY1) : 0);
 }
+// the in-step projection's scratch lies below the spectral tables in every form
+static_assert(NSLOT * P1 * 10 >= PT_SCRATCH, "projection scratch exceeds the record ring");
 
 // the thread's (at most two) record positions: pass A = its own column
 // (rows 0..7, cols 0..31), pass B = rows 8..9 and columns 32..33
@@ -446,7 +590,8 @@ __device__ __forceinline__ RecPos rec_pos(int tid, int j) {
 // PIPE (SP only): the next plane's pulls are issued before this plane's
 // collision, so two planes of loads are in flight per thread.
 template <typename ST, bool RES, bool LES, int FMODE, bool SP = false, bool PIPE = false>
-__device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int bx, int by, int bz, unsigned nblk) {
+__device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int bx, int by, int z0, int z1, float& bmin,
+                                           float& bmax, bool& bad) {
     constexpr bool FORCE = FMODE != F_NONE;
     constexpr bool SPEC = FMODE == F_SPECTRAL;
     constexpr int NSTG = LES ? 4 : 1;                    // staged fields: phi (+ u1, u2, u3)
@@ -464,8 +609,7 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
     const int nx = a.nx, ny = a.ny, nz = a.nz;
     const unsigned N = (unsigned)a.N;
     const unsigned nxy = (unsigned)nx * (unsigned)ny;
-    const int x0 = bx * TX, y0 = by * TY, z0 = bz * a.lz;
-    const int z1 = min(z0 + a.lz, nz);
+    const int x0 = bx * TX, y0 = by * TY;
     float mn, mx;
     if (a.visc_fixed) {
         mn = a.phi1;
@@ -497,17 +641,7 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
         xs[d] = (unsigned)pmod(gxd - 1 + d, nx);
         yr[d] = (unsigned)nx * (unsigned)pmod(gyd - 1 + d, ny);
     }
-    if (SPEC) {
-        for (int t = tid; t < SNK * EX1; t += NT) {
-            const int kxi = t / EX1, ex = t % EX1;
-            const float2 e = a.twx[pmod((kxi - SK) * pmod(x0 - 1 + ex, nx), nx)];
-            s_tx[t] = make_float2(e.x, -e.y);  // Re(C e^{i kx x}) = C . (cos, -sin)
-        }
-        for (int t = tid; t < SNK * EY1; t += NT) {
-            const int kyi = t / EY1, ey = t % EY1;
-            s_ty[t] = a.twy[pmod((kyi - SK) * pmod(y0 - 1 + ey, ny), ny)];
-        }
-    }
+    if (SPEC) tile_twiddles(a, s_tx, s_ty, x0, y0);
     // record-site values read from HBM one plane ahead (p, and u without LES)
     float pf_dp[2], pf_u[2][3];
     auto prefetch = [&](int zr) {
@@ -674,6 +808,22 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
         }
     };
 
+    // L2 prefetch of the tile's new u rows of planes z0 .. zl-1 (written
+    // planes ago, since evicted) for the in-step projection after the march
+    auto u_prefetch = [&](int zl) {
+        const int xr = min(TX, nx - x0);
+        const size_t end = ((size_t)5 * N * sizeof(float)) & ~(size_t)15;
+        for (int t = tid; t < 3 * TY * (zl - z0); t += NT) {
+            const int r = t % TY, c = (t / TY) % 3, zz = z0 + t / (3 * TY);
+            if (y0 + r >= ny) continue;
+            const size_t o = (size_t)(c + 1) * N + (size_t)zz * nxy + (size_t)(y0 + r) * nx + x0;
+            const size_t b0 = (o * sizeof(float)) & ~(size_t)15;
+            size_t b1 = ((o + xr) * sizeof(float) + 15) & ~(size_t)15;
+            if (b1 > end) b1 = end;
+            if (b1 > b0) prefetch_l2((const char*)a.maco + b0, (unsigned)(b1 - b0));
+        }
+    };
+
     // ---- prologue: records of planes z0-1, z0, z0+1 ----
     // Records of plane zr need the staged planes zr-1..zr+1; the chunk needs
     // records z0-1..z1, so planes z0-2..z1+1 are staged. Plane zz is staged
@@ -712,9 +862,6 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
     if (z0 + 3 <= z1 + 1) stage(z0 + 3);  // slot of z0-1, last read by records(z0)
     records(z0 + 1);
     if (z0 + 2 <= z1) prefetch(z0 + 2);
-
-    float bmin = INFINITY, bmax = -INFINITY;
-    bool bad = false;
 
     // g pulled from x - c_i at plane zp (the PIPE register stage)
     auto pull_g = [&](int zp, float* v) {
@@ -756,6 +903,7 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
             if (act && z + 1 < z1) pull_g(z + 1, gnx);
         }
         if (a.l2_prefetch && z + 1 < z1) pull_prefetch(z + 1);
+        if (SPEC && a.proj_in_step && z == z1 - 1) u_prefetch(z);
         if (z + 2 <= z1) records(z + 2);
         if (z + 3 <= z1) prefetch(z + 3);
         if (act) {
@@ -863,6 +1011,28 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
             bad |= !(isfinite(dphin) && isfinite(dpn) && isfinite(u1n) && isfinite(u2n) && isfinite(u3n));
         }
     }
+}
+
+// block (bx, by, bz) marches planes bz lz .. bz lz + lz - 1 of its tile, projects
+// the new u of its tile (band forcing), then the block-count finalisations
+template <typename ST, bool RES, bool LES, int FMODE, bool SP, bool PIPE = false>
+__device__ __forceinline__ void fused_grid(const FastArgs& a, float* smem) {
+    float bmin = INFINITY, bmax = -INFINITY;
+    bool bad = false;
+    const unsigned nblk = gridDim.x * gridDim.y * gridDim.z;
+    const int z0 = blockIdx.z * a.lz, z1 = min(z0 + a.lz, a.nz);
+    fused_body<ST, RES, LES, FMODE, SP, PIPE>(a, smem, blockIdx.x, blockIdx.y, z0, z1, bmin, bmax, bad);
+    if constexpr (FMODE == F_SPECTRAL) {
+        if (a.proj_in_step) {
+            // the tile's twiddle tables follow the staging and record rings (the layout of fused_body)
+            const float2* s_tx =
+                reinterpret_cast<const float2*>(smem + fused_smem_floats(LES, false, true, SP)) + 2 * 3 * SNK * EY1;
+            const int gxd = blockIdx.x * TX + (threadIdx.x % TX), gyd = blockIdx.y * TY + threadIdx.x / TX;
+            project_tile(a, smem, s_tx, s_tx + SNK * EX1, gxd, gyd, z0, z1, gxd < a.nx && gyd < a.ny,
+                         blockIdx.x + 3 * blockIdx.y + 5 * blockIdx.z);
+            spectral_block_done(a, smem, nblk);
+        }
+    }
     minmax_block_and_finalize<float>(a.st, (double)bmin, (double)bmax, a.maco, a.phi1, a.N, (double)a.phi1,
                                      (double)a.phi2, bad, a.step, nblk);
 }
@@ -871,23 +1041,20 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
 template <typename ST, bool RES, int FMODE>
 __global__ void __launch_bounds__(NT, 3) step_fused_sp(const FastArgs a) {
     extern __shared__ float smem[];
-    fused_body<ST, RES, false, FMODE, true>(a, smem, blockIdx.x, blockIdx.y, blockIdx.z,
-                                            gridDim.x * gridDim.y * gridDim.z);
+    fused_grid<ST, RES, false, FMODE, true>(a, smem);
 }
 
 // the same with the next plane's pulls in registers: two blocks per SM
 template <typename ST, bool RES, int FMODE>
 __global__ void __launch_bounds__(NT, 2) step_fused_sp_pipe(const FastArgs a) {
     extern __shared__ float smem[];
-    fused_body<ST, RES, false, FMODE, true, true>(a, smem, blockIdx.x, blockIdx.y, blockIdx.z,
-                                                  gridDim.x * gridDim.y * gridDim.z);
+    fused_grid<ST, RES, false, FMODE, true, true>(a, smem);
 }
 
 template <typename ST, bool RES, bool LES, int FMODE, bool SP = false>
 __global__ void __launch_bounds__(NT, 2) step_fused(const FastArgs a) {
     extern __shared__ float smem[];
-    fused_body<ST, RES, LES, FMODE, SP>(a, smem, blockIdx.x, blockIdx.y, blockIdx.z,
-                                        gridDim.x * gridDim.y * gridDim.z);
+    fused_grid<ST, RES, LES, FMODE, SP>(a, smem);
 }
 
 // ---- band projection of the new u (F_SPECTRAL) ---------------------------------------
@@ -1027,7 +1194,8 @@ __device__ void project_rows(const FastArgs& a, int first, int stride, int nrows
     __syncthreads();
     if (!s_last) return;
     __threadfence();
-    spectral_finalize(a);
+    __shared__ double fin[FIN_SCRATCH];
+    spectral_finalize(a, fin);
     if (tid == 0) a.st->sp_done = 0u;
 }
 
@@ -1220,6 +1388,8 @@ static void fill_fast(dl_handle* h, FastArgs& a) {
     a.nz = h->nz;
     a.lz = h->lz > 0 ? h->lz : 16;
     a.l2_prefetch = h->l2_prefetch;
+    a.proj_in_step = h->proj_in_step;
+
     a.N = (long long)h->N;
     a.st = h->d_state;
     a.phi1 = (float)P.phi1;
@@ -1426,13 +1596,18 @@ static int fast_spectral_project(dl_handle* h) {
 
 static const int PROJ_ROWS = 64;  // rows of the band projection per block (batched ensembles)
 
+static int sm_count(dl_handle* h) {
+    static int sms_of[64] = {0};
+    int& sms = sms_of[h->device & 63];
+    if (sms == 0 && cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device) != cudaSuccess) sms = 152;
+    return sms;
+}
+
 // band projection launch: four blocks on every SM (the register limit), one
 // wave; fewer blocks when there are fewer rows than warps
 static int launch_projection(dl_handle* h, const FastArgs& a) {
     const long long rows = (long long)a.ny * a.nz;
-    static int sm_count[64] = {0};
-    int& sms = sm_count[h->device & 63];
-    if (sms == 0 && cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device) != cudaSuccess) sms = 152;
+    const int sms = sm_count(h);
     const long long need = (rows + PROJ_NT / 32 - 1) / (PROJ_NT / 32);
     const unsigned grid = (unsigned)std::min<long long>(4LL * sms, need);
     DL_LAUNCH(h, false, (sp_project_fast<<<grid, PROJ_NT, 0, h->stream>>>(a)));
@@ -1469,7 +1644,7 @@ static int launch_fused(dl_handle* h, const FastArgs& a) {
         DL_LAUNCH(h, true, (step_fused<ST, RES, LES, FMODE><<<grid, NT, sm, h->stream>>>(a)));
     }
     DL_CUDA(h, cudaGetLastError());
-    if (FMODE == F_SPECTRAL) return launch_projection(h, a);
+    if (FMODE == F_SPECTRAL && !a.proj_in_step) return launch_projection(h, a);
     return DL_OK;
 }
 
@@ -1577,7 +1752,12 @@ __global__ void __launch_bounds__(NT, 2) step_batched(const FastArgs* __restrict
         int* dst = (int*)&s_a;
         for (int t = threadIdx.x; t < (int)(sizeof(FastArgs) / sizeof(int)); t += blockDim.x) dst[t] = src[t];
         __syncthreads();
-        fused_body<ST, RES, LES, FMODE>(s_a, smem, it.y, it.z, it.w, nblk_of[it.x]);
+        float bmin = INFINITY, bmax = -INFINITY;
+        bool bad = false;
+        const int z0 = it.w * s_a.lz;
+        fused_body<ST, RES, LES, FMODE, false>(s_a, smem, it.y, it.z, z0, min(z0 + s_a.lz, s_a.nz), bmin, bmax, bad);
+        minmax_block_and_finalize<float>(s_a.st, (double)bmin, (double)bmax, s_a.maco, s_a.phi1, s_a.N,
+                                         (double)s_a.phi1, (double)s_a.phi2, bad, s_a.step, nblk_of[it.x]);
     }
 }
 
@@ -1746,7 +1926,10 @@ static int batch_build(BatchImpl* b) {
     for (int m = 0; m < nm; ++m) {
         dl_handle* h = b->mem[m];
         h->lz = min(b->lz, h->nz);
-        for (int k = 0; k < 2; ++k) make_step_args(h, k, b->h_table[(size_t)k * nm + m]);
+        for (int k = 0; k < 2; ++k) {
+            make_step_args(h, k, b->h_table[(size_t)k * nm + m]);
+            b->h_table[(size_t)k * nm + m].proj_in_step = 0;  // the batch projects in its own launch
+        }
         const int gx = (h->nx + TX - 1) / TX, gy = (h->ny + TY - 1) / TY, gz = (h->nz + h->lz - 1) / h->lz;
         nblk[m] = (unsigned)(gx * gy * gz);
     }

@@ -269,8 +269,13 @@ int dl_profile_read(dl_handle* h, dl_profile_stats* out);
 
 /* Launch-shape knobs of the fused kernel (no reference counterpart: the
  * reference fixes its loop structure at compile time). key "lz": z planes
- * marched by one block (1..nz); "lz" = 0 restores the default. Read back with
- * dl_get_option. Returns DL_ERR_ARG for an unknown key or value. */
+ * marched by one block (1..nz); "lz" = 0 restores the default. "prefetch" 0|1:
+ * bulk L2 prefetch of the next plane's pulled rows. "pipeline" 0|1 (single
+ * phase): the next plane's pulls held in registers. "projection" 0|1 (band
+ * forcing, default 1): the projection of the new u on the band modes done by
+ * each block of the fused step after its march, else by a launch of its own;
+ * both give the same coefficients up to the FP32 summation order. Read back
+ * with dl_get_option. Returns DL_ERR_ARG for an unknown key or value. */
 int dl_set_option(dl_handle* h, const char* key, int64_t value);
 int dl_get_option(dl_handle* h, const char* key, int64_t* value);
 

@@ -173,3 +173,24 @@ def test_minmax_async_equals_minmax(form):
         g.minmax_async(buf.data_ptr())
         g.sync()
         assert (float(buf[0]), float(buf[1])) == g.minmax()
+
+
+@pytest.mark.parametrize("form,tol_phi,tol_u", [(FORM_FP32, 1e-5, 1e-7), (FORM_FP16, 5e-4, 5e-6)])
+@pytest.mark.parametrize("shape,lz", [((32, 32, 32), 0), ((40, 20, 22), 8)])
+def test_projection_in_step_equals_own_launch(form, tol_phi, tol_u, shape, lz):
+    """The band projection of the new u done by each block of the fused step
+    after its march gives the run of the projection's own launch, up to the FP32
+    summation order (odd sizes: partial tiles in x and y, a partial z chunk).
+    Tolerances: half of the form's tolerance against the oracle."""
+    P, f, mode, force = make_case("spectral_les", shape)
+    out = {}
+    for proj in (0, 1):
+        g = Droplet(P, shape, form)
+        g.set_option("projection", proj)
+        if lz:
+            g.set_option("lz", lz)
+        start(g, f, mode, force)
+        g.step(40)
+        out[proj] = g.get_fields()
+    e = errors(P, out[1], out[0])
+    assert e["phi"] <= tol_phi and e["u"] <= tol_u and e["p"] <= tol_u, e
