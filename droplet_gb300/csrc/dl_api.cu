@@ -326,7 +326,7 @@ int dl_set_option(dl_handle* h, const char* key, int64_t value) {
     if (!h || !key) return DL_ERR_ARG;
     if (strcmp(key, "lz") == 0) {
         if (value < 0 || value > h->nz) return set_error(h, DL_ERR_ARG, "lz=%lld outside 0..nz", (long long)value);
-        h->lz = value == 0 ? 16 : (int)value;
+        h->lz = value == 0 ? (h->nz < DL_DEFAULT_LZ ? h->nz : DL_DEFAULT_LZ) : (int)value;
         return DL_OK;
     }
     if (strcmp(key, "prefetch") == 0) {

@@ -104,6 +104,10 @@ struct FastSpectral {
 
 }  // namespace dl
 
+// z planes one block of the fused kernel marches by default: the autotuner's
+// choice for the 128^3 two-phase workloads in the FP32 and FP16 forms
+constexpr int DL_DEFAULT_LZ = 32;
+
 struct dl_handle {
     dl_params P;
     int nx, ny, nz;
@@ -135,7 +139,7 @@ struct dl_handle {
     void* gs[2];
     float* mac32[2];         // [5][N]: phi - phi1, u1, u2, u3, p - 1/3
     float* force32;          // [3][N]
-    int lz;                  // z planes per block of the fused kernel
+    int lz;                  // z planes per block of the fused kernel (0: DL_DEFAULT_LZ, at most nz)
     int l2_prefetch;         // fused kernel: bulk L2 prefetch of the next plane's pulls
     int sp_pipeline;         // single-phase kernel: next plane's pulls held in registers
     int proj_in_step;        // band forcing: projection of the new u inside the fused step (else its own launch)

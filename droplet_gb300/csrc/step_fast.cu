@@ -1386,7 +1386,7 @@ static void fill_fast(dl_handle* h, FastArgs& a) {
     a.nx = h->nx;
     a.ny = h->ny;
     a.nz = h->nz;
-    a.lz = h->lz > 0 ? h->lz : 16;
+    a.lz = h->lz > 0 ? h->lz : std::min(h->nz, DL_DEFAULT_LZ);
     a.l2_prefetch = h->l2_prefetch;
     a.proj_in_step = h->proj_in_step;
 
@@ -1498,7 +1498,7 @@ int fast_alloc(dl_handle* h) {
         DL_CUDA(h, cudaMemsetAsync(h->gs[k], 0, es * Q * N, h->stream));
         DL_CUDA(h, cudaMemsetAsync(h->mac32[k], 0, sizeof(float) * 5 * N, h->stream));
     }
-    if (h->lz <= 0) h->lz = 16;
+    if (h->lz <= 0) h->lz = std::min(h->nz, DL_DEFAULT_LZ);
     return fast_spectral_alloc(h);
 }
 
