@@ -58,7 +58,7 @@ enum { F_NONE = 0, F_ARRAY = 1, F_SPECTRAL = 2 };
 constexpr int SK = 2;                 // in-kernel spectral forcing: |k_x| <= 2 (kc <= 3)
 constexpr int SNK = 2 * SK + 1;
 constexpr int SMAXM = 64;             // at most 64 band modes (two per lane)
-constexpr int SP_NREP = 16;           // copies of the projection accumulators (block b adds to copy b % 16)
+constexpr int SP_NREP = 4;            // copies of the projection accumulators (block b adds to copy b % 4)
 
 struct FastArgs {
     int nx, ny, nz, lz;
@@ -349,17 +349,28 @@ __device__ void spectral_finalize(const FastArgs& a, double* scratch) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nv = 6 * a.nm;  // values per accumulator copy
     if (tid < a.nm) s_w[tid] = (double)__ldg(a.modes + tid).w;
-    // fold the copies (fixed order), zero them
-    for (int t = tid; t < nv; t += blockDim.x) {
-        double c[SP_NREP];  // all loads first, so that they are in flight together
+    // fold the copies (fixed order), zero them: a thread's (at most two, nv <= 6 SMAXM
+    // <= 2 blockDim.x) values in one pass, all loads in flight together
+    static_assert(6 * SMAXM <= 2 * NT, "two folded values per thread");
+    {
+        double c[2][SP_NREP];
 #pragma unroll
-        for (int r = 0; r < SP_NREP; ++r) c[r] = __ldcg(a.acc + (size_t)r * nv + t);
-        double v = c[0];
+        for (int j = 0; j < 2; ++j) {
+            const int t = tid + j * blockDim.x;
 #pragma unroll
-        for (int r = 1; r < SP_NREP; ++r) v += c[r];
+            for (int r = 0; r < SP_NREP; ++r) c[j][r] = t < nv ? __ldcg(a.acc + (size_t)r * nv + t) : 0.0;
+        }
 #pragma unroll
-        for (int r = 0; r < SP_NREP; ++r) a.acc[(size_t)r * nv + t] = 0.0;
-        s_acc[t] = v;
+        for (int j = 0; j < 2; ++j) {
+            const int t = tid + j * blockDim.x;
+            if (t >= nv) continue;
+            double v = c[j][0];
+#pragma unroll
+            for (int r = 1; r < SP_NREP; ++r) v += c[j][r];
+#pragma unroll
+            for (int r = 0; r < SP_NREP; ++r) a.acc[(size_t)r * nv + t] = 0.0;
+            s_acc[t] = v;
+        }
     }
     __syncthreads();
     double e = 0.0;
