@@ -162,6 +162,8 @@ def declare(lib: C.CDLL, prefix: str) -> None:
         lib.dl_energy.restype = C.c_int
         lib.dl_get_minmax_async.argtypes = [h, _vp]
         lib.dl_get_minmax_async.restype = C.c_int
+        lib.dl_set_minmax_mirror.argtypes = [h, _vp, C.c_int64]
+        lib.dl_set_minmax_mirror.restype = C.c_int
         lib.dl_reduce_static.argtypes = [h, C.c_int, C.POINTER(DLDiag)]
         lib.dl_reduce_static.restype = C.c_int
         lib.dl_sync.argtypes = [h]
@@ -239,6 +241,7 @@ HEADER_SYMBOLS = [
     "dl_get_step",
     "dl_get_minmax",
     "dl_get_minmax_async",
+    "dl_set_minmax_mirror",
     "dl_reduce",
     "dl_reduce_static",
     "dl_energy",

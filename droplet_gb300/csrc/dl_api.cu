@@ -87,6 +87,8 @@ static int reset_state(dl_handle* h) {
     s.phi_max = h->P.phi2;
     s.key_min = KEY_POS_INF;
     s.key_max = KEY_NEG_INF;
+    s.mirror = h->mirror_dev;
+    s.mirror_slots = h->mirror_slots;
     DL_CUDA(h, cudaMemcpyAsync(h->d_state, &s, sizeof(s), cudaMemcpyHostToDevice, h->stream));
     DL_CUDA(h, cudaStreamSynchronize(h->stream));
     return DL_OK;
@@ -574,6 +576,31 @@ int dl_get_minmax_async(dl_handle* h, double* dst) {
     if (!h || !dst) return DL_ERR_ARG;
     // phi_min and phi_max are the first two fields of the device state
     DL_CUDA(h, cudaMemcpyAsync(dst, h->d_state, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    return DL_OK;
+}
+
+int dl_set_minmax_mirror(dl_handle* h, double* host, int64_t nslots) {
+    if (!h) return DL_ERR_ARG;
+    double* dev = nullptr;
+    if (host) {
+        if (nslots < 1) return set_error(h, DL_ERR_ARG, "minmax mirror: nslots must be >= 1");
+        cudaPointerAttributes at;
+        if (cudaPointerGetAttributes(&at, host) != cudaSuccess || at.type != cudaMemoryTypeHost ||
+            !at.devicePointer) {
+            cudaGetLastError();
+            return set_error(h, DL_ERR_ARG, "minmax mirror: not page-locked host memory the device can write");
+        }
+        dev = (double*)at.devicePointer;
+    }
+    h->mirror_dev = dev;
+    h->mirror_slots = dev ? nslots : 0;
+    struct {
+        double* p;
+        long long n;
+    } v = {h->mirror_dev, h->mirror_slots};
+    DL_CUDA(h, cudaMemcpyAsync((char*)h->d_state + offsetof(DevState, mirror), &v, sizeof(v), cudaMemcpyHostToDevice,
+                               h->stream));
+    DL_CUDA(h, cudaStreamSynchronize(h->stream));
     return DL_OK;
 }
 

@@ -52,6 +52,10 @@ struct DevState {
     double sp_coef;                  // 0.5 eps / E
     unsigned int sp_done;            // last-block ticket of the band projection
     unsigned int pad2_;
+    // host mirror of every step's phi range (dl_set_minmax_mirror): the step
+    // that takes the counter to n writes mirror[2 (n % slots) + 0, 1]
+    double* mirror;                  // device address of page-locked host memory, or null
+    long long mirror_slots;
 };
 
 // Ordered mapping of a double to a signed 64-bit key (monotone for non-NaN).
@@ -143,6 +147,8 @@ struct dl_handle {
     int l2_prefetch;         // fused kernel: bulk L2 prefetch of the next plane's pulls
     int sp_pipeline;         // single-phase kernel: next plane's pulls held in registers
     int proj_in_step;        // band forcing: projection of the new u inside the fused step (else its own launch)
+    double* mirror_dev;      // dl_set_minmax_mirror: device address of the host mirror (or null)
+    long long mirror_slots;
     // dl_energy: cuFFT plan and buffers (allocated on first use)
     long long en_plan;
     int en_plan_ok;

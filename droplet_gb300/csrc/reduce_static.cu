@@ -14,13 +14,14 @@
 // time on one device (from two streams, two handles or two host threads)
 // race on it and give wrong sums: the caller serialises them.
 #include "dl_internal.cuh"
+#include "diag_site.cuh"
 
 #include <atomic>
 #include <string.h>
 
 namespace dl {
 
-constexpr int RS_NSUM = 24;  // sums, then min, max (the dl_reduce set)
+constexpr int RS_NSUM = DIAG_NSUM;  // sums, then min, max (the dl_reduce set)
 constexpr int RS_NPART = RS_NSUM + 2;
 constexpr int RS_THREADS = 256;
 constexpr int RS_MAX_BLOCKS = DL_REDUCE_STATIC_MAX_BLOCKS;
@@ -39,13 +40,8 @@ static __device__ __align__(256) double g_reduce_scratch[RS_WORDS];
 static_assert(RS_WORDS * sizeof(double) == DL_REDUCE_STATIC_SCRATCH_BYTES, "scratch size and header disagree");
 
 struct RsArgs {
-    int nx, ny, nz;
-    long long N;
-    double phi1, phi2, nu1, dnu, graddiv;
-    double phi_off, p_off;  // stored phi and p are phi - phi_off, p - p_off
+    DiagConsts k;
 };
-
-__device__ __forceinline__ long long rs_wrap(int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); }
 
 // Neumaier step: (s, c) += v
 __device__ __forceinline__ void rs_add(double& s, double& c, double v) {
@@ -66,76 +62,8 @@ __global__ void __launch_bounds__(RS_THREADS) reduce_static_kernel(const T* __re
 #pragma unroll
     for (int k = 0; k < RS_NSUM; ++k) acc[k] = 0.0;
     double vmin = INFINITY, vmax = -INFINITY;
-    const long long N = a.N;
-    const double inv = 1.0 / (a.phi2 - a.phi1);
-    const double mid = 0.5 * (a.phi1 + a.phi2);
-    for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < N; s += (long long)gridDim.x * blockDim.x) {
-        const long long row = s / a.nx;
-        const int x = (int)(s - row * a.nx);
-        const int z = (int)(row / a.ny);
-        const int y = (int)(row - (long long)z * a.ny);
-        const double ph = a.phi_off + (double)mac[s];
-        const double u1 = (double)mac[N + s], u2 = (double)mac[2 * N + s], u3 = (double)mac[3 * N + s];
-        const double p = a.p_off + (double)mac[4 * N + s];
-        // du_b/dx_a with the 14-neighbour gradient stencil: gu[b + 3a]
-        double gu[9];
-#pragma unroll
-        for (int k = 0; k < 9; ++k) gu[k] = 0.0;
-#pragma unroll
-        for (int i = 1; i < Q; ++i) {
-            const long long nb = rs_wrap(x + cx(i), a.nx) +
-                                 (long long)a.nx * (rs_wrap(y + cy(i), a.ny) + (long long)a.ny * rs_wrap(z + cz(i), a.nz));
-            const double v[3] = {(double)mac[N + nb], (double)mac[2 * N + nb], (double)mac[3 * N + nb]};
-            const double c[3] = {(double)cx(i), (double)cy(i), (double)cz(i)};
-#pragma unroll
-            for (int al = 0; al < 3; ++al)
-#pragma unroll
-                for (int be = 0; be < 3; ++be) gu[be + 3 * al] += c[al] * v[be];
-        }
-        double ss = 0.0;
-#pragma unroll
-        for (int be = 0; be < 3; ++be)
-#pragma unroll
-            for (int al = 0; al < 3; ++al) {
-                const double st = 0.5 * (gu[al + 3 * be] + gu[be + 3 * al]) / a.graddiv;
-                ss += st * st;
-            }
-        const double w = (ph - a.phi1) * inv;
-        const double nu = a.nu1 + w * a.dnu;
-        acc[0] += ph;
-        acc[1] += p;
-        acc[2] += u1;
-        acc[3] += u2;
-        acc[4] += u3;
-        acc[5] += 0.5 * (u1 * u1 + u2 * u2 + u3 * u3);
-        acc[6] += 2.0 * nu * ss;
-        acc[7] += (ph > mid) ? 1.0 : 0.0;
-        acc[8] += w;
-        if (w > 0.95) {
-            acc[9] += p;
-            acc[10] += 1.0;
-        }
-        if (w < 0.05) {
-            acc[11] += p;
-            acc[12] += 1.0;
-        }
-        const double X = (double)x, Y = (double)y, Z = (double)z;
-        acc[13] += w;
-        acc[14] += w * X;
-        acc[15] += w * Y;
-        acc[16] += w * Z;
-        acc[17] += w * X * X;
-        acc[18] += w * Y * Y;
-        acc[19] += w * Z * Z;
-        acc[20] += w * X * Y;
-        acc[21] += w * X * Z;
-        acc[22] += w * Y * Z;
-        acc[23] += (ph == ph && isfinite(ph)) ? 0.0 : 1.0;
-        if (ph == ph) {
-            vmin = fmin(vmin, ph);
-            vmax = fmax(vmax, ph);
-        }
-    }
+    diag_sites(mac, a.k, blockIdx.x * (long long)blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x, acc, vmin,
+               vmax);
 
     // block partials: warp shuffles, then one row per warp in shared memory
     __shared__ double sh[RS_THREADS / 32][RS_NPART];
@@ -240,17 +168,7 @@ static int reduce_static_any(dl_handle* h, const T* d_mac, double phi_off, doubl
     if (rc != DL_OK) return rc;
     RsArgs a;
     memset(&a, 0, sizeof(a));
-    a.nx = h->nx;
-    a.ny = h->ny;
-    a.nz = h->nz;
-    a.N = (long long)h->N;
-    a.phi1 = h->P.phi1;
-    a.phi2 = h->P.phi2;
-    a.nu1 = h->P.nu1;
-    a.dnu = h->P.nu2 - h->P.nu1;
-    a.graddiv = 10.0 * h->P.ds;
-    a.phi_off = phi_off;
-    a.p_off = p_off;
+    diag_consts(h, phi_off, p_off, a.k);
     reduce_static_kernel<T><<<nblocks, RS_THREADS, 0, h->stream>>>(d_mac, a, scratch);
     DL_CUDA(h, cudaGetLastError());
     h->launches += 1;

@@ -175,6 +175,13 @@ class _HandleAPI:
         at pinned_ptr; read them once the stream has passed this point."""
         self._call("get_minmax_async", C.c_void_p(int(pinned_ptr)))
 
+    def set_minmax_mirror(self, pinned_ptr: int, nslots: int = 2):
+        """Have every step write its (phi_min, phi_max) into 2 nslots pinned
+        host doubles at pinned_ptr: the step that takes the step counter to n
+        fills slot n % nslots once its launch completes. pinned_ptr 0 turns the
+        mirror off."""
+        self._call("set_minmax_mirror", C.c_void_p(int(pinned_ptr) or None), C.c_int64(int(nslots)))
+
 
 class Droplet(_HandleAPI):
     """Whole-domain droplet state resident on the current CUDA device."""

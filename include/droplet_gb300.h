@@ -205,6 +205,17 @@ int dl_get_minmax(dl_handle* h, double* phi_min, double* phi_max);
  * step behind while the GPU keeps stepping. */
 int dl_get_minmax_async(dl_handle* h, double* dst);
 
+/* Host mirror of every step's phi range, written by the step itself (no
+ * reference counterpart: the reference reduces phi's range on the host each
+ * step, program/lbm_drop_xy.f90 physics). With host = page-locked memory of
+ * 2 nslots doubles, the step that takes the step counter to n writes
+ * host[2 (n % nslots)] = phi_min and host[2 (n % nslots) + 1] = phi_max; the
+ * values are there once that step's launch has completed (an event recorded
+ * after dl_step). No copy is enqueued. host = NULL switches the mirror off.
+ * Returns DL_ERR_ARG if host is not page-locked memory the device can write
+ * or nslots < 1. */
+int dl_set_minmax_mirror(dl_handle* h, double* host, int64_t nslots);
+
 /* FP64 diagnostics of the current fields; replaces the ad-hoc sums of the
  * analysis programs (kinetic.d in program/lbm_iht_xy.f90:777-822, the
  * droplet moments of prototype_program/two-phase/drop8_mpi.f90:812-970). */

@@ -194,3 +194,33 @@ def test_projection_in_step_equals_own_launch(form, tol_phi, tol_u, shape, lz):
         out[proj] = g.get_fields()
     e = errors(P, out[1], out[0])
     assert e["phi"] <= tol_phi and e["u"] <= tol_u and e["p"] <= tol_u, e
+
+
+@pytest.mark.parametrize("form", [FORM_FP64, FORM_FP32, FORM_FP16])
+def test_minmax_mirror_holds_every_step(form):
+    """dl_set_minmax_mirror: the step that takes the counter to n writes its
+    phi range into slot n % nslots of the pinned mirror, the values that
+    dl_get_minmax returns after it; off again, the steps write nothing; memory
+    that is not page-locked is refused on the host."""
+    import torch
+
+    from droplet_gb300 import DropletError
+
+    shape = (24, 20, 16)
+    P, f, mode, force = make_case("plain", shape)
+    g = Droplet(P, shape, form)
+    start(g, f, mode, force)
+    buf = torch.full((3, 2), -1.0, dtype=torch.float64).pin_memory()
+    g.set_minmax_mirror(buf.data_ptr(), 3)
+    for n in range(1, 8):
+        g.step(1)
+        g.sync()
+        assert (float(buf[n % 3, 0]), float(buf[n % 3, 1])) == g.minmax(), n
+    g.set_minmax_mirror(0)
+    before = buf.clone()
+    g.step(2)
+    g.sync()
+    assert torch.equal(buf, before)
+    pageable = np.zeros(4)
+    with pytest.raises(DropletError):
+        g.set_minmax_mirror(pageable.ctypes.data, 2)
