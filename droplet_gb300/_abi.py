@@ -164,6 +164,10 @@ def declare(lib: C.CDLL, prefix: str) -> None:
         lib.dl_get_minmax_async.restype = C.c_int
         lib.dl_set_minmax_mirror.argtypes = [h, _vp, C.c_int64]
         lib.dl_set_minmax_mirror.restype = C.c_int
+        lib.dl_host_alloc.argtypes = [C.c_int64, C.POINTER(_vp)]
+        lib.dl_host_alloc.restype = C.c_int
+        lib.dl_host_free.argtypes = [_vp]
+        lib.dl_host_free.restype = C.c_int
         lib.dl_reduce_static.argtypes = [h, C.c_int, C.POINTER(DLDiag)]
         lib.dl_reduce_static.restype = C.c_int
         lib.dl_sync.argtypes = [h]
@@ -242,6 +246,8 @@ HEADER_SYMBOLS = [
     "dl_get_minmax",
     "dl_get_minmax_async",
     "dl_set_minmax_mirror",
+    "dl_host_alloc",
+    "dl_host_free",
     "dl_reduce",
     "dl_reduce_static",
     "dl_energy",

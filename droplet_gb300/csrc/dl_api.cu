@@ -604,6 +604,27 @@ int dl_set_minmax_mirror(dl_handle* h, double* host, int64_t nslots) {
     return DL_OK;
 }
 
+int dl_host_alloc(int64_t bytes, void** out) {
+    if (!out || bytes < 0) return DL_ERR_ARG;
+    *out = nullptr;
+    void* p = nullptr;
+    if (cudaHostAlloc(&p, bytes > 0 ? (size_t)bytes : 1, cudaHostAllocMapped) != cudaSuccess) {
+        cudaGetLastError();
+        return DL_ERR_ALLOC;
+    }
+    memset(p, 0, bytes > 0 ? (size_t)bytes : 1);
+    *out = p;
+    return DL_OK;
+}
+
+int dl_host_free(void* p) {
+    if (p && cudaFreeHost(p) != cudaSuccess) {
+        cudaGetLastError();
+        return DL_ERR_ARG;
+    }
+    return DL_OK;
+}
+
 int dl_sync(dl_handle* h) {
     if (!h) return DL_ERR_ARG;
     DL_CUDA(h, cudaStreamSynchronize(h->stream));

@@ -216,6 +216,13 @@ int dl_get_minmax_async(dl_handle* h, double* dst);
  * or nslots < 1. */
 int dl_set_minmax_mirror(dl_handle* h, double* host, int64_t nslots);
 
+/* Page-locked host memory the device can write (for dl_set_minmax_mirror and
+ * the *_async host buffers) for hosts without the CUDA runtime headers, e.g.
+ * a Fortran main loop: *out receives bytes of zeroed memory; release with
+ * dl_host_free. Returns DL_ERR_ALLOC if the allocation fails. */
+int dl_host_alloc(int64_t bytes, void** out);
+int dl_host_free(void* p);
+
 /* FP64 diagnostics of the current fields; replaces the ad-hoc sums of the
  * analysis programs (kinetic.d in program/lbm_iht_xy.f90:777-822, the
  * droplet moments of prototype_program/two-phase/drop8_mpi.f90:812-970). */

@@ -69,8 +69,25 @@ int main(int argc, char** argv) {
     }
     check(h, dl_set_fields(h, f[0], f[1], f[2], f[3], f[4]), "dl_set_fields");
     check(h, dl_init_equilibrium(h), "dl_init_equilibrium");
-    check(h, dl_step(h, steps), "dl_step");
-    check(h, dl_sync(h), "dl_sync");
+    /* every step's phi range in a page-locked mirror of 2 slots, checked
+     * against dl_get_minmax after each step */
+    double* mirror = NULL;
+    check(h, dl_host_alloc(4 * sizeof(double), (void**)&mirror), "dl_host_alloc");
+    check(h, dl_set_minmax_mirror(h, mirror, 2), "dl_set_minmax_mirror");
+    int mismatches = 0;
+    for (int k = 1; k <= steps; ++k) {
+        check(h, dl_step(h, 1), "dl_step");
+        check(h, dl_sync(h), "dl_sync");
+        double mn, mx;
+        check(h, dl_get_minmax(h, &mn, &mx), "dl_get_minmax");
+        if (mirror[2 * (k % 2)] != mn || mirror[2 * (k % 2) + 1] != mx) ++mismatches;
+    }
+    check(h, dl_set_minmax_mirror(h, NULL, 0), "dl_set_minmax_mirror");
+    check(h, dl_host_free(mirror), "dl_host_free");
+    if (mismatches) {
+        fprintf(stderr, "minmax mirror: %d of %d steps differ from dl_get_minmax\n", mismatches, steps);
+        return 1;
+    }
     dl_diag d;
     check(h, dl_reduce(h, &d), "dl_reduce");
     printf("%.17g %.17g %.17g %.17g %.17g %.17g %.17g %.17g %lld\n", d.phi_sum, d.p_sum, d.mom[0], d.mom[1],
