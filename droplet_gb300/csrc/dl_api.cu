@@ -87,8 +87,6 @@ static int reset_state(dl_handle* h) {
     s.phi_max = h->P.phi2;
     s.key_min = KEY_POS_INF;
     s.key_max = KEY_NEG_INF;
-    s.mirror = h->mirror_dev;
-    s.mirror_slots = h->mirror_slots;
     DL_CUDA(h, cudaMemcpyAsync(h->d_state, &s, sizeof(s), cudaMemcpyHostToDevice, h->stream));
     DL_CUDA(h, cudaStreamSynchronize(h->stream));
     return DL_OK;
@@ -476,12 +474,27 @@ int dl_set_force(dl_handle* h, int mode, const double* fx, const double* fy, con
     return DL_OK;
 }
 
+// one warp after a step: its phi range into slot `slot` of the host mirror. A
+// launch of its own, because any code added to the step kernels' shared
+// finalisation changes their register allocation (a store there made the FP16
+// step 5 % slower)
+__global__ void mirror_copy(const DevState* __restrict__ st, double* __restrict__ m, long long slot) {
+    if (threadIdx.x == 0) {
+        m[2 * slot] = st->phi_min;
+        m[2 * slot + 1] = st->phi_max;
+    }
+}
+
 int dl_step(dl_handle* h, int nsteps) {
     if (!h || nsteps < 0) return DL_ERR_ARG;
     if (!h->eq_init) return set_error(h, DL_ERR_STATE, "dl_step before dl_init_equilibrium / dl_set_populations");
     for (int k = 0; k < nsteps; ++k) {
         int rc = is_fast(h) ? fast_step(h) : fp64_step(h);
         if (rc != DL_OK) return rc;
+        if (h->mirror_dev) {
+            DL_LAUNCH(h, false, (mirror_copy<<<1, 32, 0, h->stream>>>(h->d_state, h->mirror_dev, h->step & h->mirror_mask)));
+            DL_CUDA(h, cudaGetLastError());
+        }
     }
     return DL_OK;
 }
@@ -583,7 +596,8 @@ int dl_set_minmax_mirror(dl_handle* h, double* host, int64_t nslots) {
     if (!h) return DL_ERR_ARG;
     double* dev = nullptr;
     if (host) {
-        if (nslots < 1) return set_error(h, DL_ERR_ARG, "minmax mirror: nslots must be >= 1");
+        if (nslots < 1 || (nslots & (nslots - 1)))
+            return set_error(h, DL_ERR_ARG, "minmax mirror: nslots must be a power of two");
         cudaPointerAttributes at;
         if (cudaPointerGetAttributes(&at, host) != cudaSuccess || at.type != cudaMemoryTypeHost ||
             !at.devicePointer) {
@@ -593,14 +607,7 @@ int dl_set_minmax_mirror(dl_handle* h, double* host, int64_t nslots) {
         dev = (double*)at.devicePointer;
     }
     h->mirror_dev = dev;
-    h->mirror_slots = dev ? nslots : 0;
-    struct {
-        double* p;
-        long long n;
-    } v = {h->mirror_dev, h->mirror_slots};
-    DL_CUDA(h, cudaMemcpyAsync((char*)h->d_state + offsetof(DevState, mirror), &v, sizeof(v), cudaMemcpyHostToDevice,
-                               h->stream));
-    DL_CUDA(h, cudaStreamSynchronize(h->stream));
+    h->mirror_mask = dev ? nslots - 1 : 0;
     return DL_OK;
 }
 

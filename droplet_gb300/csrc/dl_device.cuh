@@ -136,11 +136,6 @@ __device__ bool minmax_block_and_finalize(DevState* st, double vmin, double vmax
     if (threadIdx.x == 0) {
         st->phi_min = s_mn;
         st->phi_max = s_mx;
-        if (st->mirror) {  // visible to the host once the launch has completed
-            const long long sl = step % st->mirror_slots;
-            st->mirror[2 * sl] = s_mn;
-            st->mirror[2 * sl + 1] = s_mx;
-        }
         st->key_min = KEY_POS_INF;
         st->key_max = KEY_NEG_INF;
         __threadfence();

@@ -52,10 +52,6 @@ struct DevState {
     double sp_coef;                  // 0.5 eps / E
     unsigned int sp_done;            // last-block ticket of the band projection
     unsigned int pad2_;
-    // host mirror of every step's phi range (dl_set_minmax_mirror): the step
-    // that takes the counter to n writes mirror[2 (n % slots) + 0, 1]
-    double* mirror;                  // device address of page-locked host memory, or null
-    long long mirror_slots;
 };
 
 // Ordered mapping of a double to a signed 64-bit key (monotone for non-NaN).
@@ -148,7 +144,7 @@ struct dl_handle {
     int sp_pipeline;         // single-phase kernel: next plane's pulls held in registers
     int proj_in_step;        // band forcing: projection of the new u inside the fused step (else its own launch)
     double* mirror_dev;      // dl_set_minmax_mirror: device address of the host mirror (or null)
-    long long mirror_slots;
+    long long mirror_mask;   // its slots - 1 (slots a power of two)
     // dl_energy: cuFFT plan and buffers (allocated on first use)
     long long en_plan;
     int en_plan_ok;

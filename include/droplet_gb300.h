@@ -205,15 +205,16 @@ int dl_get_minmax(dl_handle* h, double* phi_min, double* phi_max);
  * step behind while the GPU keeps stepping. */
 int dl_get_minmax_async(dl_handle* h, double* dst);
 
-/* Host mirror of every step's phi range, written by the step itself (no
- * reference counterpart: the reference reduces phi's range on the host each
- * step, program/lbm_drop_xy.f90 physics). With host = page-locked memory of
- * 2 nslots doubles, the step that takes the step counter to n writes
- * host[2 (n % nslots)] = phi_min and host[2 (n % nslots) + 1] = phi_max; the
- * values are there once that step's launch has completed (an event recorded
- * after dl_step). No copy is enqueued. host = NULL switches the mirror off.
+/* Host mirror of every step's phi range (no reference counterpart: the
+ * reference reduces phi's range on the host each step, program/lbm_drop_xy.f90
+ * physics). With host = page-locked memory of 2 nslots doubles, dl_step
+ * follows each step with a one-warp kernel that writes, for the step that
+ * takes the step counter to n, host[2 (n % nslots)] = phi_min and
+ * host[2 (n % nslots) + 1] = phi_max (no copy-engine transfer); the values
+ * are there once an event recorded after dl_step has completed. host = NULL
+ * switches the mirror off.
  * Returns DL_ERR_ARG if host is not page-locked memory the device can write
- * or nslots < 1. */
+ * or nslots is not a power of two (1, 2, 4, ...). */
 int dl_set_minmax_mirror(dl_handle* h, double* host, int64_t nslots);
 
 /* Page-locked host memory the device can write (for dl_set_minmax_mirror and

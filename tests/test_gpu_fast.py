@@ -210,12 +210,14 @@ def test_minmax_mirror_holds_every_step(form):
     P, f, mode, force = make_case("plain", shape)
     g = Droplet(P, shape, form)
     start(g, f, mode, force)
-    buf = torch.full((3, 2), -1.0, dtype=torch.float64).pin_memory()
-    g.set_minmax_mirror(buf.data_ptr(), 3)
-    for n in range(1, 8):
+    buf = torch.full((4, 2), -1.0, dtype=torch.float64).pin_memory()
+    g.set_minmax_mirror(buf.data_ptr(), 4)
+    for n in range(1, 10):
         g.step(1)
         g.sync()
-        assert (float(buf[n % 3, 0]), float(buf[n % 3, 1])) == g.minmax(), n
+        assert (float(buf[n % 4, 0]), float(buf[n % 4, 1])) == g.minmax(), n
+    with pytest.raises(DropletError):
+        g.set_minmax_mirror(buf.data_ptr(), 3)  # not a power of two
     g.set_minmax_mirror(0)
     before = buf.clone()
     g.step(2)
