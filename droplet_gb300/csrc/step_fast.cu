@@ -241,7 +241,7 @@ __device__ __forceinline__ Rec make_record(const FastArgs& a, float dphi, const 
         const float t = 2.f * ss;
         nut = t > 0.f ? a.csd * (t * rsqrtf(t)) : 0.f;
     }
-    r.omg = __frcp_rn(0.5f + 3.f * (nu + nut) * a.inv_ds + a.anu23);
+    r.omg = __fdividef(1.f, 0.5f + 3.f * (nu + nut) * a.inv_ds + a.anu23);  // tau_g in [0.5, 10]: no special cases
     r.Fx = r.Fy = r.Fz = 0.f;
     return r;
 }
@@ -287,7 +287,7 @@ __device__ __forceinline__ Rec make_record_les2(const FastArgs& a, float dphi, c
     const float ss = gu[0] * gu[0] + gu[4] * gu[4] + gu[8] * gu[8] + 2.f * (sxy * sxy + sxz * sxz + syz * syz);
     const float t = 2.f * ss;
     const float nut = t > 0.f ? a.csd * (t * rsqrtf(t)) : 0.f;
-    r.omg = __frcp_rn(0.5f + 3.f * (nu + nut) * a.inv_ds + a.anu23);
+    r.omg = __fdividef(1.f, 0.5f + 3.f * (nu + nut) * a.inv_ds + a.anu23);  // tau_g in [0.5, 10]: no special cases
     r.Fx = r.Fy = r.Fz = 0.f;
     return r;
 }
@@ -1019,7 +1019,7 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
             const float phin_f = a.phi1 + dphin;
             bmin = fminf(bmin, phin_f);  // fminf ignores NaN
             bmax = fmaxf(bmax, phin_f);
-            bad |= !(isfinite(dphin) && isfinite(dpn) && isfinite(u1n) && isfinite(u2n) && isfinite(u3n));
+            bad |= !isfinite(dphin + dpn + u1n + u2n + u3n);  // a NaN or infinity in any term reaches the sum
         }
     }
 }
