@@ -143,11 +143,16 @@ __device__ __forceinline__ float csumf(const float* v) {
 }
 
 // p0(phi) - p0(phi1) without cancellation:
-// dphi [T / ((1 - b phi)(1 - b phi1)) - a (phi + phi1)]
+// dphi [T / ((1 - b phi)(1 - b phi1)) - a (phi + phi1)]. Every operation is
+// rounded explicitly, so the writer and the reader of the FP16 residual basis
+// (RES) get the same bits; RES takes the approximate reciprocal (deterministic;
+// den lies in (0.3, 1) for the reference parameter sets), which made the FP16
+// step 1.3 % faster and the FP32 step slower, so FP32 keeps the rounded one
+template <bool RES>
 __device__ __forceinline__ float site_dp0(const FastArgs& a, float dphi) {
     const float phi = __fadd_rn(a.phi1, dphi);
     const float den = __fmul_rn(__fmaf_rn(-a.b, phi, 1.f), a.omb1);
-    const float t = __fmul_rn(a.T, __frcp_rn(den));  // reciprocal, not a full division
+    const float t = __fmul_rn(a.T, RES ? __fdividef(1.f, den) : __frcp_rn(den));
     return __fmul_rn(dphi, __fmaf_rn(-a.a, __fadd_rn(phi, a.phi1), t));
 }
 
@@ -203,7 +208,7 @@ struct Rec {
 };
 
 // v[1..14]: dphi at the D3Q15 neighbours; w[c][1..14]: u_c there (LES only)
-template <bool LES>
+template <bool LES, bool RES>
 __device__ __forceinline__ Rec make_record(const FastArgs& a, float dphi, const float* v, const float (*w)[Q],
                                            float u1, float u2, float u3, float dp, float mn, float kscale) {
     Rec r;
@@ -216,7 +221,7 @@ __device__ __forceinline__ Rec make_record(const FastArgs& a, float dphi, const 
     r.gz = csumf<2>(v) * a.inv_grad;
     r.gsq = r.gx * r.gx + r.gy * r.gy + r.gz * r.gz;
     const float phi = __fadd_rn(a.phi1, dphi);
-    r.dp0 = site_dp0(a, dphi);
+    r.dp0 = site_dp0<RES>(a, dphi);
     r.dA = r.dp0 - a.kf * phi * lap - a.kf6 * r.gsq;
     r.dphi = dphi;
     r.u1 = u1;
@@ -248,6 +253,7 @@ __device__ __forceinline__ Rec make_record(const FastArgs& a, float dphi, const 
 
 // the LES record from pairs (phi - phi1, u1) and (u2, u3) at the 14 neighbours:
 // the same sums as make_record<true>, two fields per packed instruction
+template <bool RES>
 __device__ __forceinline__ Rec make_record_les2(const FastArgs& a, float dphi, const float2* pa, const float2* pb,
                                                 float u1, float u2, float u3, float dp, float mn, float kscale) {
     Rec r;
@@ -262,7 +268,7 @@ __device__ __forceinline__ Rec make_record_les2(const FastArgs& a, float dphi, c
     r.gz = az.x * a.inv_grad;
     r.gsq = r.gx * r.gx + r.gy * r.gy + r.gz * r.gz;
     const float phi = __fadd_rn(a.phi1, dphi);
-    r.dp0 = site_dp0(a, dphi);
+    r.dp0 = site_dp0<RES>(a, dphi);
     r.dA = r.dp0 - a.kf * phi * lap - a.kf6 * r.gsq;
     r.dphi = dphi;
     r.u1 = u1;
@@ -779,7 +785,7 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
                 }
                 const float2 ca = reinterpret_cast<const float2*>(stc)[c2];
                 const float2 cb = reinterpret_cast<const float2*>(stc + 2 * P2)[c2];
-                r = make_record_les2(a, ca.x, pa, pb, ca.y, cb.x, cb.y, pf_dp[j], mn, kscale);
+                r = make_record_les2<RES>(a, ca.x, pa, pb, ca.y, cb.x, cb.y, pf_dp[j], mn, kscale);
             } else {
                 float v[Q];
 #pragma unroll
@@ -787,7 +793,7 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
                     const float* st = cz(i) == 0 ? stc : (cz(i) > 0 ? stp : stm);
                     v[i] = st[c2 + cy(i) * EX2 + cx(i)];
                 }
-                r = make_record<false>(a, stc[c2], v, nullptr, pf_u[j][0], pf_u[j][1], pf_u[j][2], pf_dp[j], mn,
+                r = make_record<false, RES>(a, stc[c2], v, nullptr, pf_u[j][0], pf_u[j][1], pf_u[j][2], pf_dp[j], mn,
                                        kscale);
             }
             s_q0[o] = make_float4(r.dphi, r.u1, r.u2, r.u3);
@@ -996,7 +1002,7 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
             const unsigned d = zo[1] + yr[1] + xs[1];
             if (RES) {
                 const float phin = __fadd_rn(a.phi1, dphin);
-                const float dp0n = site_dp0(a, dphin);
+                const float dp0n = site_dp0<RES>(a, dphin);
                 const float Sn = site_S(dpn, u1n, u2n, u3n);
 #pragma unroll
                 for (int i = 0; i < Q; ++i) {
@@ -1234,7 +1240,7 @@ __global__ void __launch_bounds__(256) init_fast(const FastArgs a) {
         v[i] = a.mac[nb];
     }
     const float u1 = a.mac[N + s], u2 = a.mac[2 * N + s], u3 = a.mac[3 * N + s], dp = a.mac[4 * N + s];
-    const Rec r = make_record<false>(a, a.mac[s], v, nullptr, u1, u2, u3, dp, a.phi1, a.dnu / (a.phi2 - a.phi1));
+    const Rec r = make_record<false, RES>(a, a.mac[s], v, nullptr, u1, u2, u3, dp, a.phi1, a.dnu / (a.phi2 - a.phi1));
     const float phi = __fadd_rn(a.phi1, r.dphi);
 #pragma unroll
     for (int i = 0; i < Q; ++i) {
@@ -1285,7 +1291,7 @@ __global__ void pops_to_host(const FastArgs a, double* __restrict__ fa, double* 
     const float dphi = a.mac[s], u1 = a.mac[N + s], u2 = a.mac[2 * N + s], u3 = a.mac[3 * N + s];
     const float dp = a.mac[4 * N + s];
     const float phi = __fadd_rn(a.phi1, dphi);
-    const float dp0 = site_dp0(a, dphi);
+    const float dp0 = site_dp0<RES>(a, dphi);
     const float S = site_S(dp, u1, u2, u3);
     const double E[3] = {2.0 / 9.0, 1.0 / 9.0, 1.0 / 72.0};
 #pragma unroll
@@ -1330,7 +1336,7 @@ __global__ void pops_from_host(const FastArgs a, const double* __restrict__ fa, 
     a.maco[3 * N + s] = u3;
     a.maco[4 * N + s] = dp;
     const float phi = __fadd_rn(a.phi1, dphi);
-    const float dp0 = site_dp0(a, dphi);
+    const float dp0 = site_dp0<RES>(a, dphi);
     const float S = site_S(dp, u1, u2, u3);
 #pragma unroll
     for (int i = 0; i < Q; ++i) {
