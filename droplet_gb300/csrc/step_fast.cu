@@ -246,7 +246,7 @@ __device__ __forceinline__ Rec make_record(const FastArgs& a, float dphi, const 
         const float t = 2.f * ss;
         nut = t > 0.f ? a.csd * (t * rsqrtf(t)) : 0.f;
     }
-    r.omg = __fdividef(1.f, 0.5f + 3.f * (nu + nut) * a.inv_ds + a.anu23);  // tau_g in [0.5, 10]: no special cases
+    r.omg = __fdividef(1.f, 0.5f + 3.f * (nu + nut) * a.inv_ds + a.anu23);  // tau_g >= 0.5 and far below 2^126, where the approximate division is within 2 ulp
     r.Fx = r.Fy = r.Fz = 0.f;
     return r;
 }
@@ -293,7 +293,7 @@ __device__ __forceinline__ Rec make_record_les2(const FastArgs& a, float dphi, c
     const float ss = gu[0] * gu[0] + gu[4] * gu[4] + gu[8] * gu[8] + 2.f * (sxy * sxy + sxz * sxz + syz * syz);
     const float t = 2.f * ss;
     const float nut = t > 0.f ? a.csd * (t * rsqrtf(t)) : 0.f;
-    r.omg = __fdividef(1.f, 0.5f + 3.f * (nu + nut) * a.inv_ds + a.anu23);  // tau_g in [0.5, 10]: no special cases
+    r.omg = __fdividef(1.f, 0.5f + 3.f * (nu + nut) * a.inv_ds + a.anu23);  // tau_g >= 0.5 and far below 2^126, where the approximate division is within 2 ulp
     r.Fx = r.Fy = r.Fz = 0.f;
     return r;
 }
