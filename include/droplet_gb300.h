@@ -211,8 +211,9 @@ int dl_get_minmax_async(dl_handle* h, double* dst);
  * follows each step with a one-warp kernel that writes, for the step that
  * takes the step counter to n, host[2 (n % nslots)] = phi_min and
  * host[2 (n % nslots) + 1] = phi_max (no copy-engine transfer); the values
- * are there once an event recorded after dl_step has completed. host = NULL
- * switches the mirror off.
+ * are there once an event recorded after dl_step has completed. The array
+ * must stay allocated until the mirror is switched off (host = NULL) or the
+ * handle is destroyed. Steps taken by dl_batch_step do not write it.
  * Returns DL_ERR_ARG if host is not page-locked memory the device can write
  * or nslots is not a power of two (1, 2, 4, ...). */
 int dl_set_minmax_mirror(dl_handle* h, double* host, int64_t nslots);
