@@ -108,10 +108,25 @@ def tune_droplet(sim, steps: int = 20, use_cache: bool = True) -> dict:
     return dict(res, cached=False)
 
 
+def _wall_steps(obj, steps: int) -> float:
+    """Wall-clock ms per step of obj.step(steps) between two syncs (the members'
+    launches overlap, so summed kernel times would not rank the shapes)."""
+    import time
+
+    obj.step(2)
+    obj.sync()
+    t0 = time.perf_counter()
+    obj.step(steps)
+    obj.sync()
+    return (time.perf_counter() - t0) * 1e3 / steps
+
+
 def tune_ensemble(ens, steps: int = 10, use_cache: bool = True) -> dict:
-    """Pick "lz" and "blocks_per_sm" for an Ensemble."""
+    """Pick "lz" (and, for the persistent launch, "blocks_per_sm") for an
+    Ensemble in its current mode."""
     shapes = [(m.nx, m.ny, m.nz) for m in ens.members]
-    key = _key("batch", ens.form, shapes, f"les{int(bool(ens.members[0].params.les))}")
+    persistent = int(ens.get_option("persistent"))
+    key = _key("batch", ens.form, shapes, f"les{int(bool(ens.members[0].params.les))}_p{persistent}")
     if use_cache:
         hit = _load().get(key)
         if hit:
@@ -120,11 +135,11 @@ def tune_ensemble(ens, steps: int = 10, use_cache: bool = True) -> dict:
             return dict(hit, cached=True)
     best = None
     timings = {}
-    for bps in BPS_CANDIDATES:
+    for bps in (BPS_CANDIDATES if persistent else (2,)):
         for lz in LZ_CANDIDATES:
             ens.set_option("lz", lz)
             ens.set_option("blocks_per_sm", bps)
-            ms = _time_steps(ens, steps)
+            ms = _time_steps(ens, steps) if persistent else _wall_steps(ens, steps)
             timings[f"lz{lz}_bps{bps}"] = ms
             if best is None or ms < best[2]:
                 best = (lz, bps, ms)

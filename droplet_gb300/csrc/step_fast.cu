@@ -1796,6 +1796,8 @@ __global__ void __launch_bounds__(PROJ_NT) sp_project_batched(const FastArgs* __
     }
 }
 
+constexpr int BATCH_WORKERS = 16;  // concurrent mode: streams the members' steps are spread over
+
 struct BatchImpl {
     int nm;
     int form;
@@ -1809,6 +1811,10 @@ struct BatchImpl {
     unsigned* d_pnblk;      // projection blocks per member
     int npitems;
     int lz, bps, use_graph;
+    int persistent;         // 1: one persistent launch per step over all members; 0: the members' own steps, concurrent
+    int nworkers;           // concurrent mode: worker streams (created on first use)
+    cudaStream_t workers[BATCH_WORKERS];
+    cudaEvent_t fork, join[BATCH_WORKERS];
     int sms;
     cudaStream_t stream;
     cudaStream_t cap_stream;  // owned stream the graph is captured on (the legacy default stream cannot capture)
@@ -1865,9 +1871,10 @@ int batch_create(dl_handle** members, int nm, void** out) {
     b->nm = nm;
     b->form = h0->form;
     b->mem = members;
-    b->lz = 8;
+    b->lz = DL_DEFAULT_LZ;
     b->bps = 2;
     b->use_graph = 1;
+    b->persistent = 0;
     b->stream = h0->stream;
     b->built_parity = -1;
     b->les = h0->P.les != 0;
@@ -1892,6 +1899,11 @@ void batch_destroy(void* p) {
     if (!b) return;
     if (b->graph_ok) cudaGraphExecDestroy(b->gexec);
     if (b->cap_stream) cudaStreamDestroy(b->cap_stream);
+    for (int w = 0; w < b->nworkers; ++w) {
+        cudaStreamDestroy(b->workers[w]);
+        cudaEventDestroy(b->join[w]);
+    }
+    if (b->nworkers) cudaEventDestroy(b->fork);
     cudaFree(b->d_table);
     cudaFree(b->d_items);
     cudaFree(b->d_nblk);
@@ -1911,6 +1923,9 @@ int batch_set_option(void* p, const char* key, long long v) {
         b->bps = (int)v;
     } else if (strcmp(key, "graph") == 0) {
         b->use_graph = v ? 1 : 0;
+    } else if (strcmp(key, "persistent") == 0) {
+        if (v < 0 || v > 1) return DL_ERR_ARG;
+        b->persistent = (int)v;
     } else {
         return DL_ERR_ARG;
     }
@@ -1923,6 +1938,7 @@ int batch_get_option(void* p, const char* key, long long* v) {
     if (strcmp(key, "lz") == 0) *v = b->lz;
     else if (strcmp(key, "blocks_per_sm") == 0) *v = b->bps;
     else if (strcmp(key, "graph") == 0) *v = b->use_graph;
+    else if (strcmp(key, "persistent") == 0) *v = b->persistent;
     else return DL_ERR_ARG;
     return DL_OK;
 }
@@ -2017,8 +2033,49 @@ static int batch_build(BatchImpl* b) {
     return DL_OK;
 }
 
+// concurrent mode: every member takes its own one-launch steps (the single-
+// handle path, kernel arguments in constant memory, band projection in the
+// step) on one of up to BATCH_WORKERS streams forked from member 0's stream
+// and joined back to it at the end; members of any size, parity and force mode
+static int batch_step_concurrent(BatchImpl* b, int nsteps) {
+    dl_handle* h0 = b->mem[0];
+    const int nm = b->nm;
+    for (int m = 0; m < nm; ++m)
+        if (!b->mem[m]->eq_init) return set_error(h0, DL_ERR_STATE, "member %d not initialised", m);
+    if (!b->nworkers) {
+        const int nw = std::min(nm, BATCH_WORKERS);
+        DL_CUDA(h0, cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+        for (int w = 0; w < nw; ++w) {
+            DL_CUDA(h0, cudaStreamCreateWithFlags(&b->workers[w], cudaStreamNonBlocking));
+            DL_CUDA(h0, cudaEventCreateWithFlags(&b->join[w], cudaEventDisableTiming));
+            b->nworkers = w + 1;
+        }
+    }
+    const int nw = b->nworkers;
+    cudaStream_t home = h0->stream;
+    DL_CUDA(h0, cudaEventRecord(b->fork, home));
+    for (int w = 0; w < nw; ++w) DL_CUDA(h0, cudaStreamWaitEvent(b->workers[w], b->fork, 0));
+    int rc = DL_OK;
+    for (int s = 0; s < nsteps && rc == DL_OK; ++s)
+        for (int m = 0; m < nm && rc == DL_OK; ++m) {
+            dl_handle* h = b->mem[m];
+            h->lz = std::min(b->lz, h->nz);
+            cudaStream_t own = h->stream;
+            h->stream = b->workers[m % nw];
+            rc = fast_step(h);
+            h->stream = own;
+        }
+    // join even after an error, so that the home stream never runs ahead of the workers
+    for (int w = 0; w < nw; ++w) {
+        DL_CUDA(h0, cudaEventRecord(b->join[w], b->workers[w]));
+        DL_CUDA(h0, cudaStreamWaitEvent(home, b->join[w], 0));
+    }
+    return rc;
+}
+
 int batch_step(void* p, int nsteps) {
     BatchImpl* b = (BatchImpl*)p;
+    if (!b->persistent) return batch_step_concurrent(b, nsteps);
     dl_handle* h0 = b->mem[0];
     const int nm = b->nm;
     // members step together: same parity and step count, same kernel variant

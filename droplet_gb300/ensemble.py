@@ -1,5 +1,8 @@
 """Batched ensembles: many independent droplet domains (uneven sizes, their
-own parameters and seeds) stepped together by one persistent launch per step,
+own parameters and seeds) stepped together: by default each member takes its
+own one-launch steps on one of up to 16 streams forked from the ensemble's
+stream (the blocks of many members fill the GPU together); option
+"persistent" = 1 runs one persistent launch per step over all members instead,
 with pairs of steps replayed from a captured CUDA graph.
 
 The reference's analogues are replica groups of MPI ranks
@@ -81,10 +84,18 @@ class Ensemble:
         return int(v.value)
 
     def profile(self, enable: bool = True):
-        self.members[0].profile(enable)
+        for m in self.members:
+            m.profile(enable)
 
     def profile_read(self) -> dict:
-        return self.members[0].profile_read()
+        """Launch counts and event-timed durations summed over the members (the
+        persistent mode counts its launches on member 0; with concurrent member
+        launches the summed durations exceed the wall time)."""
+        tot = None
+        for m in self.members:
+            s = m.profile_read()
+            tot = dict(s) if tot is None else {k: tot[k] + s[k] for k in tot}
+        return tot
 
     def sync(self):
         for m in self.members:

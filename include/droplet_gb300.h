@@ -369,12 +369,18 @@ int dl_batch_member(dl_batch* b, int m, dl_handle** member);
 /* Run every member's work on this cudaStream_t. */
 int dl_batch_set_stream(dl_batch* b, void* cuda_stream);
 
-/* Advance every member by nsteps steps. Launch accounting (dl_profile) is
- * recorded on member 0's handle. */
+/* Advance every member by nsteps steps. Default: each member takes its own
+ * one-launch steps (as dl_step) on one of up to 16 streams forked from the
+ * batch stream and joined back to it before the call returns (the blocks of
+ * many members fill the GPU together; launch accounting on each member's
+ * handle). With "persistent" = 1: one persistent launch per step over all
+ * members' tiles (members in step with each other; accounting on member 0). */
 int dl_batch_step(dl_batch* b, int nsteps);
 
-/* Knobs: "lz" z planes per work item; "blocks_per_sm" persistent blocks per
- * SM (1 or 2); "graph" 1 = replay step pairs from a CUDA graph. */
+/* Knobs: "persistent" 0|1 (the mode above, default 0); "lz" z planes per
+ * block or work item (default 32, at most a member's nz); "blocks_per_sm"
+ * persistent blocks per SM (1 or 2); "graph" 1 = replay step pairs of the
+ * persistent launch from a CUDA graph. */
 int dl_batch_set_option(dl_batch* b, const char* key, int64_t value);
 int dl_batch_get_option(dl_batch* b, const char* key, int64_t* value);
 

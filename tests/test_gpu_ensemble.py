@@ -1,7 +1,8 @@
-"""Batched ensembles: one persistent launch per step over members of uneven
-sizes and parameters must give each member the result it gets when stepped on
-its own (bitwise without spectral forcing, whose FP64 accumulation order is
-not fixed; within FP32 rounding with it)."""
+"""Batched ensembles over members of uneven sizes and parameters, in both
+modes: the members' own steps launched concurrently (the default) and one
+persistent launch per step. Each member must get the result it gets when
+stepped on its own (bitwise without spectral forcing, whose FP64 accumulation
+order is not fixed; within FP32 rounding with it)."""
 import numpy as np
 import pytest
 
@@ -35,11 +36,14 @@ def start(sim, f, spectral):
 
 
 @pytest.mark.parametrize("form", [FORM_FP32, FORM_FP16])
-@pytest.mark.parametrize("spectral,les,graph,steps", [(False, False, 1, 7), (False, True, 0, 6),
-                                                      (True, True, 1, 9)])
-def test_ensemble_matches_members_stepped_alone(form, spectral, les, graph, steps):
+@pytest.mark.parametrize("persistent,spectral,les,graph,steps", [(1, False, False, 1, 7), (1, False, True, 0, 6),
+                                                                 (1, True, True, 1, 9), (0, False, True, 0, 7),
+                                                                 (0, True, True, 0, 9)])
+def test_ensemble_matches_members_stepped_alone(form, persistent, spectral, les, graph, steps):
     cases = [member_case(m, s, spectral, les) for m, s in enumerate(SHAPES)]
     ens = Ensemble([c[0] for c in cases], SHAPES, form)
+    ens.set_option("persistent", persistent)
+    assert ens.get_option("persistent") == persistent
     ens.set_option("graph", graph)
     ens.set_option("lz", 8)
     for mem, (P, f) in zip(ens.members, cases):
@@ -63,7 +67,7 @@ def test_ensemble_matches_members_stepped_alone(form, spectral, les, graph, step
 def test_ensemble_options_and_state_checks():
     cases = [member_case(m, s, False, False) for m, s in enumerate(SHAPES[:2])]
     ens = Ensemble([c[0] for c in cases], SHAPES[:2], FORM_FP32)
-    for opt, val in (("lz", 4), ("blocks_per_sm", 1), ("graph", 0)):
+    for opt, val in (("lz", 4), ("blocks_per_sm", 1), ("graph", 0), ("persistent", 1), ("persistent", 0)):
         ens.set_option(opt, val)
         assert ens.get_option(opt) == val
     from droplet_gb300 import DropletError
