@@ -21,7 +21,7 @@ from .solver import Droplet, FORM_FP32
 class _Member(Droplet):
     """A member handle owned by its ensemble (not destroyed on close)."""
 
-    def __init__(self, lib, handle, params, shape, form):  # noqa: D401 - bypass Droplet.__init__
+    def __init__(self, lib, handle, params, shape, form, persistent):  # noqa: D401 - bypass Droplet.__init__
         nx, ny, nz = (int(v) for v in shape)
         self.nx, self.ny, self.nz = nx, ny, nz
         self.params = params
@@ -29,12 +29,17 @@ class _Member(Droplet):
         self._lib = lib
         self._cparams = params.to_c()
         self._h = handle
+        self._persistent = persistent  # callable: is the ensemble in its persistent mode?
 
     def close(self):
         self._h = None
 
     def step(self, n: int = 1):
-        raise DropletError(_abi.DL_ERR_STATE, "member step", "members step through Ensemble.step")
+        """A member may step on its own while the ensemble steps its members'
+        own launches (the default); the persistent launch needs them in step."""
+        if self._persistent():
+            raise DropletError(_abi.DL_ERR_STATE, "member step", "members step through Ensemble.step")
+        super().step(n)
 
 
 class Ensemble:
@@ -58,7 +63,8 @@ class Ensemble:
         for m in range(n):
             h = C.c_void_p()
             self._chk(self._lib.dl_batch_member(b, m, C.byref(h)), "dl_batch_member")
-            self.members.append(_Member(self._lib, h, params_list[m], shapes[m], form))
+            self.members.append(_Member(self._lib, h, params_list[m], shapes[m], form,
+                                        lambda: bool(self.get_option("persistent"))))
 
     def _chk(self, rc, what):
         if rc != 0:

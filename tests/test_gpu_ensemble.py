@@ -74,3 +74,26 @@ def test_ensemble_options_and_state_checks():
 
     with pytest.raises(DropletError):
         ens.step(1)  # members not initialised
+
+
+def test_concurrent_members_need_not_be_in_step():
+    """The default mode steps each member from its own state: member 0 taken one
+    step ahead alone, then the whole ensemble stepped, ends where a solo run of
+    one more step ends (bitwise, no spectral forcing), the others as solo runs."""
+    cases = [member_case(m, s, False, True) for m, s in enumerate(SHAPES)]
+    ens = Ensemble([c[0] for c in cases], SHAPES, FORM_FP32)
+    assert ens.get_option("persistent") == 0
+    ens.set_option("lz", 8)
+    for mem, (P, f) in zip(ens.members, cases):
+        start(mem, f, False)
+    ens.members[0].step(1)
+    ens.step(5)
+    for m, (mem, (P, f)) in enumerate(zip(ens.members, cases)):
+        solo = Droplet(P, SHAPES[m], FORM_FP32)
+        solo.set_option("lz", 8)
+        start(solo, f, False)
+        solo.step(6 if m == 0 else 5)
+        a, b = mem.get_fields(), solo.get_fields()
+        for k in ("phi", "u1", "u2", "u3", "p"):
+            assert np.array_equal(a[k], b[k]), (m, k)
+        assert mem.step_count == (6 if m == 0 else 5)
