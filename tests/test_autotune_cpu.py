@@ -44,3 +44,58 @@ def test_tuner_picks_fastest_and_caches(tmp_path, monkeypatch):
     sim2 = FakeSim()
     r2 = autotune.tune_droplet(sim2, steps=5)
     assert r2["cached"] and sim2.lz == 8 and sim2.prefetch == 1 and sim2.steps == 0
+
+
+class FakeEnsemble:
+    """Looks like an Ensemble to the tuner: lz = 16 is fastest by wall clock in the
+    concurrent mode; lz = 8 with 2 blocks per SM by launch time in the persistent one."""
+
+    def __init__(self, persistent):
+        class M:
+            nx = ny = nz = 48
+
+            class params:
+                les = True
+
+        self.members = [M(), M()]
+        self.form = 32
+        self.opts = {"lz": 32, "blocks_per_sm": 2, "persistent": persistent}
+        self.steps = 0
+        self.clock = 0.0
+
+    def get_option(self, k):
+        return self.opts[k]
+
+    def set_option(self, k, v):
+        assert k in ("lz", "blocks_per_sm")
+        self.opts[k] = v
+
+    def step(self, n):
+        lz, bps = self.opts["lz"], self.opts["blocks_per_sm"]
+        cost = 1.0 + abs(lz - 16) / 16.0 if not self.opts["persistent"] else 1.0 + abs(lz - 8) / 8.0 + (bps != 2)
+        self.clock += n * cost * 1e-3
+        self.steps += n
+
+    def sync(self):
+        pass
+
+    def profile(self, on):
+        self.steps = 0
+
+    def profile_read(self):
+        lz, bps = self.opts["lz"], self.opts["blocks_per_sm"]
+        return {"main_ms": self.steps * (1.0 + abs(lz - 8) / 8.0 + (bps != 2))}
+
+
+def test_ensemble_tuner_times_concurrent_members_by_wall_clock(tmp_path, monkeypatch):
+    monkeypatch.setenv("DROPLET_GB300_TUNE_CACHE", str(tmp_path / "tune.json"))
+    monkeypatch.setattr(autotune, "gpu_name", lambda: "fake-gpu")
+    ens = FakeEnsemble(persistent=0)
+    monkeypatch.setattr("time.perf_counter", lambda: ens.clock)
+    r = autotune.tune_ensemble(ens, steps=4)
+    assert r["lz"] == 16 and ens.opts["lz"] == 16 and ens.opts["blocks_per_sm"] == 2
+    assert set(r["timings"]) == {f"lz{lz}_bps2" for lz in autotune.LZ_CANDIDATES}
+    pers = FakeEnsemble(persistent=1)
+    r2 = autotune.tune_ensemble(pers, steps=4)
+    assert r2["lz"] == 8 and r2["blocks_per_sm"] == 2 and not r2["cached"]
+    assert len(json.load(open(tmp_path / "tune.json"))) == 2  # one cache entry per mode
