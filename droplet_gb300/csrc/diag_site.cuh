@@ -9,11 +9,11 @@
 // (prototype_program/two-phase/drop8_mpi.f90:812-970), FP64 throughout.
 //
 // The stencil weights are -1, 0, +1, so the gradient is formed by signed
-// additions only (a product with a zero weight is never issued), in the
-// storage type of the fields (FP32 for the FP32 and FP16 forms, as their step
-// forms the LES strain; FP64 for the FP64 form), and S:S is summed in FP64
-// over the six distinct entries of the symmetric strain with one scale factor
-// 1/(4 graddiv^2): GB300's FP64 pipe is narrow.
+// additions only (a product with a zero weight is never issued); it and the
+// strain contraction S:S (over the six distinct entries of the symmetric
+// strain) are formed in the storage type of the fields (FP32 for the FP32 and
+// FP16 forms, as their step forms the LES strain; FP64 for the FP64 form),
+// then scaled by 1/(4 graddiv^2) in FP64: GB300's FP64 pipe is narrow.
 #pragma once
 
 #include "dl_internal.cuh"
@@ -68,12 +68,10 @@ __device__ __forceinline__ void diag_site(const T* __restrict__ mac, const DiagC
                 else if (c[al] < 0) g[be + 3 * al] -= v[be];
             }
     }
-    double gu[9];
-#pragma unroll
-    for (int j = 0; j < 9; ++j) gu[j] = (double)g[j];
-    const double d01 = gu[1] + gu[3], d02 = gu[2] + gu[6], d12 = gu[5] + gu[7];
-    const double ss = k.sfac * (4.0 * (gu[0] * gu[0] + gu[4] * gu[4] + gu[8] * gu[8]) +
-                                2.0 * (d01 * d01 + d02 * d02 + d12 * d12));
+    // S:S before the scale, in the storage type (for FP64 fields the FP64 expression)
+    const T d01 = g[1] + g[3], d02 = g[2] + g[6], d12 = g[5] + g[7];
+    const T sT = T(4) * (g[0] * g[0] + g[4] * g[4] + g[8] * g[8]) + T(2) * (d01 * d01 + d02 * d02 + d12 * d12);
+    const double ss = k.sfac * (double)sT;
     const double w = (ph - k.phi1) * k.inv_span;
     const double nu = k.nu1 + w * k.dnu;
     acc[0] += ph;
