@@ -2055,6 +2055,13 @@ static int batch_step_concurrent(BatchImpl* b, int nsteps) {
     cudaStream_t home = h0->stream;
     DL_CUDA(h0, cudaEventRecord(b->fork, home));
     for (int w = 0; w < nw; ++w) DL_CUDA(h0, cudaStreamWaitEvent(b->workers[w], b->fork, 0));
+    // a member with a stream of its own: its worker also waits for that stream
+    // (work the caller enqueued there, e.g. set-up copies)
+    for (int m = 0; m < nm; ++m)
+        if (b->mem[m]->stream != home) {
+            DL_CUDA(h0, cudaEventRecord(b->fork, b->mem[m]->stream));
+            DL_CUDA(h0, cudaStreamWaitEvent(b->workers[m % nw], b->fork, 0));
+        }
     int rc = DL_OK;
     for (int s = 0; s < nsteps && rc == DL_OK; ++s)
         for (int m = 0; m < nm && rc == DL_OK; ++m) {
@@ -2065,11 +2072,14 @@ static int batch_step_concurrent(BatchImpl* b, int nsteps) {
             rc = fast_step(h);
             h->stream = own;
         }
-    // join even after an error, so that the home stream never runs ahead of the workers
+    // join even after an error, so that the home stream (and a member's own stream)
+    // never runs ahead of the workers
     for (int w = 0; w < nw; ++w) {
         DL_CUDA(h0, cudaEventRecord(b->join[w], b->workers[w]));
         DL_CUDA(h0, cudaStreamWaitEvent(home, b->join[w], 0));
     }
+    for (int m = 0; m < nm; ++m)
+        if (b->mem[m]->stream != home) DL_CUDA(h0, cudaStreamWaitEvent(b->mem[m]->stream, b->join[m % nw], 0));
     return rc;
 }
 

@@ -97,3 +97,25 @@ def test_concurrent_members_need_not_be_in_step():
         for k in ("phi", "u1", "u2", "u3", "p"):
             assert np.array_equal(a[k], b[k]), (m, k)
         assert mem.step_count == (6 if m == 0 else 5)
+
+
+def test_concurrent_members_on_their_own_streams():
+    """Members whose handles carry streams of their own (set-up enqueued there):
+    the batched steps wait for those streams and the members' streams see the
+    results, so every member still equals its solo run."""
+    import torch
+
+    cases = [member_case(m, s, True, True) for m, s in enumerate(SHAPES)]
+    ens = Ensemble([c[0] for c in cases], SHAPES, FORM_FP32)
+    streams = [torch.cuda.Stream() for _ in SHAPES]
+    for mem, st, (P, f) in zip(ens.members, streams, cases):
+        mem.set_stream(st.cuda_stream)
+        start(mem, f, True)
+    ens.step(6)
+    for m, (mem, (P, f)) in enumerate(zip(ens.members, cases)):
+        solo = Droplet(P, SHAPES[m], FORM_FP32)
+        start(solo, f, True)
+        solo.step(6)
+        a, b = mem.get_fields(), solo.get_fields()
+        for k in ("phi", "u1", "u2", "u3", "p"):
+            assert np.abs(a[k] - b[k]).max() <= 1e-5 * max(1.0, np.abs(b[k]).max()), (m, k)
