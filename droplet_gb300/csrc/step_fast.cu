@@ -34,10 +34,12 @@
 //   F_SPECTRAL the band forcing of program/lbm_drop_iht_xy.f90:722-842 done
 //              inside the step: the force at each record site is synthesised
 //              from the band coefficients through a per-plane table in shared
-//              memory, and the band projection of the new u is accumulated in
-//              the epilogue (a warp-level separable DFT along x, one set of
-//              FP64 atomics per block); the last block turns it into the
-//              next step's coefficients. No force array touches HBM.
+//              memory; after its march each block projects the new u of its
+//              own tile on the band modes (column sums over z for kz = 0..2,
+//              then rows over x and modes over y in shared memory, one set of
+//              FP64 atomics per block; option "projection" = 0: a launch of
+//              its own, sp_project_fast), and the last block turns the sums
+//              into the next step's coefficients. No force array touches HBM.
 #include "dl_internal.cuh"
 #include "dl_device.cuh"
 
