@@ -1754,10 +1754,15 @@ int fast_step(dl_handle* h) {
 }
 
 // ---- batched ensembles ----------------------------------------------------------
-// Every member's tiles are work items of ONE persistent launch per step; each
-// block copies its member's arguments into shared memory and runs the same
-// fused body; each member keeps its own reduction state, so its last block
-// finalises it. Optionally two steps are captured in a CUDA graph and replayed.
+// Two modes (batch option "persistent"). Default: every member takes its own
+// one-launch steps on one of up to BATCH_WORKERS streams (batch_step_concurrent).
+// Persistent: every member's tiles are work items of ONE persistent launch per
+// step; each block copies its member's arguments into shared memory and runs
+// the same fused body; each member keeps its own reduction state, so its last
+// block finalises it. Optionally two steps are captured in a CUDA graph and
+// replayed. (The persistent kernel is the slower of the two: its arguments in
+// shared memory cost it registers, and its band projection is a launch of its
+// own.)
 template <typename ST, bool RES, bool LES, int FMODE>
 __global__ void __launch_bounds__(NT, 2) step_batched(const FastArgs* __restrict__ table,
                                                       const int4* __restrict__ items, int nitems,
