@@ -26,12 +26,14 @@ int check_cuda(dl_handle* h, cudaError_t e, const char* what) {
 }
 
 void launch_begin(dl_handle* h) {
-    if (!h->prof_on) return;
+    h->prof_sample = h->prof_on && (h->launches % h->prof_on) == 0;
+    if (!h->prof_sample) return;
     if (h->prof_n == h->prof_cap) {
         int cap = h->prof_cap ? 2 * h->prof_cap : 256;
         void* p = realloc(h->prof, sizeof(dl_handle::ProfEv) * cap);
         if (!p) {
             h->prof_on = 0;
+            h->prof_sample = 0;
             return;
         }
         h->prof = (dl_handle::ProfEv*)p;
@@ -46,7 +48,8 @@ void launch_begin(dl_handle* h) {
 
 void launch_end(dl_handle* h, bool main_kernel) {
     h->launches += 1;
-    if (!h->prof_on) return;
+    if (!h->prof_sample) return;
+    h->prof_sample = 0;
     cudaEventRecord(h->prof[h->prof_n].b, h->stream);
     h->prof[h->prof_n].main = main_kernel ? 1 : 0;
     h->prof_n += 1;
@@ -210,7 +213,9 @@ int dl_destroy(dl_handle* h) {
 int dl_profile(dl_handle* h, int enable) {
     if (!h) return DL_ERR_ARG;
     DL_CUDA(h, cudaStreamSynchronize(h->stream));
-    h->prof_on = enable ? 1 : 0;
+    if (enable < 0) return set_error(h, DL_ERR_ARG, "dl_profile: enable must be >= 0");
+    h->prof_on = enable;
+    h->prof_sample = 0;
     h->prof_n = 0;
     h->launches = 0;
     return DL_OK;

@@ -167,7 +167,8 @@ struct dl_handle {
 
     // launch accounting (dl_profile)
     int64_t launches;
-    int prof_on;
+    int prof_on;             // 0: off; n > 0: events around every n-th launch
+    int prof_sample;         // the launch in flight is timed
     struct ProfEv {
         cudaEvent_t a, b;
         int main;

@@ -89,9 +89,9 @@ class Ensemble:
         self._chk(self._lib.dl_batch_get_option(self._b, key.encode(), C.byref(v)), "dl_batch_get_option")
         return int(v.value)
 
-    def profile(self, enable: bool = True):
+    def profile(self, enable: bool = True, every: int = 1):
         for m in self.members:
-            m.profile(enable)
+            m.profile(enable, every)
 
     def profile_read(self) -> dict:
         """Launch counts and event-timed durations summed over the members (the

@@ -257,9 +257,10 @@ class Droplet(_HandleAPI):
                    C.byref(n), _ptr(vols), C.c_int64(max_volumes))
         return vols[: min(int(n.value), max_volumes)].copy(), lab
 
-    def profile(self, enable: bool = True):
-        """Bracket every launch with CUDA events (and reset the counters)."""
-        self._call("profile", 1 if enable else 0)
+    def profile(self, enable: bool = True, every: int = 1):
+        """Bracket every ``every``-th launch with CUDA events (and reset the
+        counters); ``enable`` False stops."""
+        self._call("profile", int(every) if enable else 0)
 
     def set_option(self, key: str, value: int):
         """Launch-shape knob of the fused kernel (e.g. "lz")."""

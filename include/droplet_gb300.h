@@ -278,8 +278,10 @@ int dl_reduce_static(dl_handle* h, int nblocks, dl_diag* out);
 /* Wait for all work of the handle; returns the first deferred error. */
 int dl_sync(dl_handle* h);
 
-/* Bracket every kernel launch of the handle with CUDA events on its stream
- * (enable != 0) or stop doing so; resets the counters. The reference times
+/* Bracket kernel launches of the handle with CUDA events on its stream:
+ * enable = n > 0 times every n-th launch (1: every launch; a larger n keeps the
+ * events' own cost out of a timed run while still sampling it), 0 stops; resets
+ * the counters (launches counts every launch either way). The reference times
  * its loop with MPI_Wtime and writes time.d (program/lbm_drop_xy.f90:785-864);
  * this is the per-kernel device-side equivalent. */
 int dl_profile(dl_handle* h, int enable);

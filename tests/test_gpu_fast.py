@@ -155,6 +155,10 @@ def test_fast_form_profile_counts_launches():
     g.step(7)
     s = g.profile_read()
     assert s["main_launches"] == 7 and s["launches"] == 7 and s["main_ms"] > 0
+    g.profile(True, every=3)  # launches 0, 3, 6 timed, all counted
+    g.step(7)
+    s = g.profile_read()
+    assert s["main_launches"] == 3 and s["timed_launches"] == 3 and s["launches"] == 7 and s["main_ms"] > 0
 
 
 @pytest.mark.parametrize("form", [FORM_FP64, FORM_FP32])
