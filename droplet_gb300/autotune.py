@@ -1,10 +1,13 @@
 """Autotuner for the launch shape of the fused step.
 
 The tunable knobs are those of the C-ABI: for one domain the number of z
-planes a block marches ("lz", ``dl_set_option``); for an ensemble also the
-number of persistent blocks per SM ("blocks_per_sm", ``dl_batch_set_option``).
-Each candidate is timed with the library's own per-launch CUDA events after a
-few warm-up steps; the fastest is applied and cached in a JSON file keyed by
+planes a block marches ("lz", ``dl_set_option``), the bulk L2 prefetch
+("prefetch") and, for the single-phase step, "pipeline"; for an ensemble "lz"
+and, with its persistent launch, the number of blocks per SM
+("blocks_per_sm", ``dl_batch_set_option``). Each candidate is timed after a
+few warm-up steps, with the library's own per-launch CUDA events (one domain,
+persistent ensemble) or by wall clock (members launched concurrently, whose
+kernels overlap); the fastest is applied and cached in a JSON file keyed by
 the GPU, the form and the member shapes, so later runs reuse it without
 timing. The cache lives at $DROPLET_GB300_TUNE_CACHE or
 ~/.cache/droplet_gb300/tune.json.
