@@ -13,10 +13,17 @@
 // The array is shared by every handle on a device. Calls that overlap in
 // time on one device (from two streams, two handles or two host threads)
 // race on it and give wrong sums: the caller serialises them.
+//
+// The array's device address belongs to the CUDA context that loaded this
+// library's module. It is looked up on the first call in each context of a
+// device and kept with that context's id; after a cudaDeviceReset (a new
+// primary context, the module loaded again, possibly elsewhere) the next call
+// looks it up again.
 #include "dl_internal.cuh"
 #include "diag_site.cuh"
 
-#include <atomic>
+#include <cuda.h>
+#include <mutex>
 #include <string.h>
 
 namespace dl {
@@ -27,13 +34,15 @@ constexpr int RS_THREADS = 256;
 constexpr int RS_MAX_BLOCKS = DL_REDUCE_STATIC_MAX_BLOCKS;
 constexpr int RS_DEFAULT_BLOCKS = 304;  // 2 x 152 SMs
 constexpr int RS_SEGS = 8;              // block-order segments of the final sum
+static_assert(RS_NPART * RS_SEGS <= RS_THREADS, "the last block folds one (value, segment) pair per thread");
 
 // Layout, in doubles: [0, RS_MAX_BLOCKS * RS_NPART) per-block partials,
 // then RS_NPART results, then one 64-bit arrival counter. 253,144 bytes.
 // Nothing in the partials or the results has to start at zero: every call
-// writes them before it reads them. The counter must be zero when a call
-// starts: the array is zero when the library is loaded, and the last block
-// of every call puts the counter back to zero.
+// writes them before it reads them. The counter must be zero when the
+// launch starts: every call clears it on its stream just before the launch
+// (an 8-byte memset, which allocates nothing), and the last block of a
+// launch that ran to its end also puts it back to zero.
 constexpr size_t RS_WORDS = (size_t)RS_MAX_BLOCKS * RS_NPART + RS_NPART + 1;
 static __device__ __align__(256) double g_reduce_scratch[RS_WORDS];
 
@@ -140,24 +149,63 @@ __global__ void __launch_bounds__(RS_THREADS) reduce_static_kernel(const T* __re
     if (threadIdx.x == 0) atomicExch(arrivals, 0ull);  // ready for the next call
 }
 
-// Device address of g_reduce_scratch, looked up once per device (with that
-// device current) and kept. Concurrent first calls may both look it up; they
-// store the same value.
+// Device address of g_reduce_scratch per device, valid for the context whose
+// id it is stored with. The driver's context calls are reached through the
+// runtime's entry-point query, so the library needs no link to libcuda.
 constexpr int RS_MAX_DEVICES = 64;
-static std::atomic<double*> g_scratch_addr[RS_MAX_DEVICES];
+struct RsAddr {
+    unsigned long long ctx_id;
+    double* addr;
+};
+static RsAddr g_scratch_addr[RS_MAX_DEVICES];
+static std::mutex g_scratch_mutex;
+
+typedef CUresult (*RsCtxGetCurrent)(CUcontext*);
+typedef CUresult (*RsCtxGetId)(CUcontext, unsigned long long*);
+
+// id of the calling thread's current context (the device's primary context,
+// made current by the caller); false when it cannot be read
+static bool current_context_id(unsigned long long* id) {
+    static RsCtxGetCurrent get_current = nullptr;
+    static RsCtxGetId get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<RsCtxGetCurrent>(fn);
+        fn = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<RsCtxGetId>(fn);
+    });
+    if (!get_current || !get_id) return false;
+    CUcontext ctx = nullptr;
+    if (get_current(&ctx) != CUDA_SUCCESS || ctx == nullptr) return false;
+    return get_id(ctx, id) == CUDA_SUCCESS;
+}
 
 static int scratch_address(dl_handle* h, double** out) {
     if (h->device < 0 || h->device >= RS_MAX_DEVICES)
         return set_error(h, DL_ERR_UNSUPPORTED, "dl_reduce_static supports device ordinals below %d", RS_MAX_DEVICES);
-    double* p = g_scratch_addr[h->device].load(std::memory_order_acquire);
-    if (!p) {
-        void* addr = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&addr, g_reduce_scratch);
-        if (e != cudaSuccess) return check_cuda(h, e, "cudaGetSymbolAddress(g_reduce_scratch)");
-        p = static_cast<double*>(addr);
-        g_scratch_addr[h->device].store(p, std::memory_order_release);
+    // the handle's device is current (dl_reduce_static makes it so), and its
+    // primary context exists since dl_create
+    unsigned long long id = 0;
+    const bool have_id = current_context_id(&id);
+    std::lock_guard<std::mutex> lock(g_scratch_mutex);
+    RsAddr& c = g_scratch_addr[h->device];
+    if (have_id && c.addr && c.ctx_id == id) {
+        *out = c.addr;
+        return DL_OK;
     }
-    *out = p;
+    void* addr = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&addr, g_reduce_scratch);
+    if (e != cudaSuccess) return check_cuda(h, e, "cudaGetSymbolAddress(g_reduce_scratch)");
+    // without a context id the address is looked up on every call
+    c.ctx_id = have_id ? id : 0;
+    c.addr = have_id ? static_cast<double*>(addr) : nullptr;
+    *out = static_cast<double*>(addr);
     return DL_OK;
 }
 
@@ -169,6 +217,9 @@ static int reduce_static_any(dl_handle* h, const T* d_mac, double phi_off, doubl
     RsArgs a;
     memset(&a, 0, sizeof(a));
     diag_consts(h, phi_off, p_off, a.k);
+    // the arrival counter starts at zero whatever an earlier launch left
+    DL_CUDA(h, cudaMemsetAsync(scratch + (size_t)RS_MAX_BLOCKS * RS_NPART + RS_NPART, 0, sizeof(unsigned long long),
+                               h->stream));
     reduce_static_kernel<T><<<nblocks, RS_THREADS, 0, h->stream>>>(d_mac, a, scratch);
     DL_CUDA(h, cudaGetLastError());
     h->launches += 1;

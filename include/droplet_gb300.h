@@ -266,9 +266,12 @@ int dl_fp64_ceiling(dl_handle* h, double* tflops);
  * same fields with the same nblocks return identical values; they agree with
  * dl_reduce to rounding (the order of the final additions differs).
  *
- * The first call on each device looks up the array's device address (once,
- * with that device made current for the call); make that first call before
- * any stream capture starts on the device. Calls on one device must not
+ * The first call on each device looks up the array's device address (once
+ * per CUDA context of the device, with that device made current for the
+ * call; after a cudaDeviceReset the next call looks it up again); make that
+ * first call before any stream capture starts on the device. Each call clears
+ * the array's 8-byte arrival counter on h's stream before its launch (a
+ * memset, no allocation). Calls on one device must not
  * overlap in time (two streams, two handles or two host threads at once):
  * they share the array and would race. The call synchronises h's stream. */
 #define DL_REDUCE_STATIC_MAX_BLOCKS 1216

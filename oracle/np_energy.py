@@ -51,3 +51,40 @@ def free_energy_sums(P, phi):
     mu = (P.T * lg + P.T / omb - 2.0 * P.a * phi) - P.kappag * lap
     gsq = (g[0] * g[0] + g[1] * g[1] + g[2] * g[2]) / (10.0 * P.ds) ** 2
     return float(psi.sum()), float(mu.sum()), float(gsq.sum())
+
+
+def dissipation_sum(P, u1, u2, u3, phi):
+    """Sum over sites of 2 nu(phi) S:S (program/energy_budget.f90:1494), with
+    grad u from the 14-neighbour stencil of various_cal
+    (program/lbm_drop_xy.f90:615-633) and nu(phi) linear in
+    w = (phi - phi1)/(phi2 - phi1) between nu1 and nu2."""
+    u = (u1, u2, u3)
+    G = [[np.zeros_like(u1) for _ in range(3)] for _ in range(3)]  # G[a][b] = d u_b / d x_a
+    for i in range(1, 15):
+        for b in range(3):
+            v = shifted(u[b], i)
+            for a in range(3):
+                if CR[i][a] != 0.0:
+                    G[a][b] = G[a][b] + CR[i][a] * v
+    gd = 10.0 * P.ds
+    G = [[G[a][b] / gd for b in range(3)] for a in range(3)]
+    ss = sum(G[a][a] * G[a][a] for a in range(3))
+    for a, b in ((0, 1), (0, 2), (1, 2)):
+        s = 0.5 * (G[a][b] + G[b][a])
+        ss = ss + 2.0 * s * s
+    w = (phi - P.phi1) / (P.phi2 - P.phi1)
+    nu = P.nu1 + w * (P.nu2 - P.nu1)
+    return float((2.0 * nu * ss).sum())
+
+
+def second_moments(P, phi):
+    """w_sum, w_x (x, y, z) and w_xx (xx, yy, zz, xy, xz, yz) of
+    w = (phi - phi1)/(phi2 - phi1) over the sites, coordinates = site indices."""
+    nz, ny, nx = phi.shape
+    z, y, x = np.meshgrid(np.arange(nz, dtype=np.float64), np.arange(ny, dtype=np.float64),
+                          np.arange(nx, dtype=np.float64), indexing="ij")
+    w = (phi - P.phi1) / (P.phi2 - P.phi1)
+    return {"w_sum": float(w.sum()),
+            "w_x": [float((w * x).sum()), float((w * y).sum()), float((w * z).sum())],
+            "w_xx": [float((w * x * x).sum()), float((w * y * y).sum()), float((w * z * z).sum()),
+                     float((w * x * y).sum()), float((w * x * z).sum()), float((w * y * z).sum())]}

@@ -1,0 +1,73 @@
+"""Long-horizon accuracy of the reduced-precision forms against the plain
+FP64 form on the GPU, on forced turbulence with a droplet (the physics of the
+128^3 workload: Smagorinsky LES, constant-injection band forcing; here at
+48^3 over 1000 steps): max phi~ error, droplet-volume drift, the kinetic-energy
+spectrum by shell (enesupe_cal, program/turbulence_hit_xy.f90:588-645) and the
+dissipation rate (program/turbulence_hit_xy.f90:426-463; both conventions
+differ by a constant factor, so one relative error covers them).
+
+Tolerances (checked at every 250 steps):
+  phi~ (= 2 (phi - phi1)/(phi2 - phi1) - 1) max error     <= 1e-3
+  |volume drift| (sum of w, relative)                     <= 2e-5
+  spectrum, L2 over shells, relative                      <= 1e-3
+  spectrum, worst shell holding >= 1e-3 of the peak       <= 1e-3
+  dissipation 2 nu <S:S>, relative                        <= 1e-3"""
+import numpy as np
+import pytest
+
+from droplet_gb300 import configs
+from droplet_gb300.solver import Droplet, FORM_FP16, FORM_FP32, FORM_FP64
+
+pytestmark = pytest.mark.gpu
+
+STEPS, EVERY = 1000, 250
+
+
+def spectrum_errors(a, b):
+    a, b = np.asarray(a[1:]), np.asarray(b[1:])
+    l2 = float(np.sqrt(((a - b) ** 2).sum() / (b * b).sum()))
+    sig = b >= 1e-3 * b.max()
+    return l2, float((np.abs(a - b)[sig] / b[sig]).max())
+
+
+@pytest.fixture(scope="module")
+def curves():
+    w = configs.forced_turbulence(n=48, radius=9.0, seed=2, steps=STEPS)
+    sims = {}
+    for form in (FORM_FP64, FORM_FP32, FORM_FP16):
+        d = Droplet(w.params, w.shape, form)
+        d.set_fields(**w.fields)
+        d.init_equilibrium()
+        d.set_force(w.force_mode)
+        sims[form] = d
+    span = w.params.phi2 - w.params.phi1
+    nb = w.shape[0] // 2 + 1
+    out = {FORM_FP32: [], FORM_FP16: []}
+    for _ in range(STEPS // EVERY):
+        for d in sims.values():
+            d.step(EVERY)
+        rf, rd, re = sims[FORM_FP64].get_fields(), sims[FORM_FP64].reduce(), sims[FORM_FP64].energy(nb)
+        for form in (FORM_FP32, FORM_FP16):
+            f, dd, e = sims[form].get_fields(), sims[form].reduce(), sims[form].energy(nb)
+            l2, mx = spectrum_errors(e["spectrum"], re["spectrum"])
+            out[form].append({
+                "phi_tilde": float(2.0 * np.abs(f["phi"] - rf["phi"]).max() / span),
+                "volume": float((dd["vol_smooth"] - rd["vol_smooth"]) / rd["vol_smooth"]),
+                "spec_l2": l2, "spec_max": mx,
+                "diss": float((dd["diss"] - rd["diss"]) / rd["diss"]),
+            })
+    for d in sims.values():
+        d.close()
+    return out
+
+
+@pytest.mark.parametrize("form", [FORM_FP32, FORM_FP16])
+def test_long_horizon_errors_against_fp64(curves, form):
+    for k, row in enumerate(curves[form]):
+        step = (k + 1) * EVERY
+        print(form, step, row)
+        assert row["phi_tilde"] <= 1e-3, (step, row)
+        assert abs(row["volume"]) <= 2e-5, (step, row)
+        assert row["spec_l2"] <= 1e-3, (step, row)
+        assert row["spec_max"] <= 1e-3, (step, row)
+        assert abs(row["diss"]) <= 1e-3, (step, row)
