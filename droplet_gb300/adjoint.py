@@ -123,6 +123,9 @@ class CheckpointedRun:
         t0 = time.perf_counter()
         if self.sim is None:
             self.sim = Droplet(self.params, self.shape, FORM_FP32)
+            # the pull form: every step's state is saved, and a push step's state
+            # would need a settle launch before each save
+            self.sim.set_option("push", 0)
             nck = 1 if self.store_all else (self.nsteps + self.S - 1) // self.S
             self.ckpt = [self._buffer("full") for _ in range(nck)]
             if self.store_all:

@@ -45,6 +45,7 @@ SOURCES = {
     "reduce_static.cu": EXACT,
     "energy.cu": EXACT,
     "step_fast.cu": FAST,
+    "step_push.cu": FAST,
     "adjoint.cu": FAST,
     "labels.cu": FAST,
     "ceiling.cu": FAST,

@@ -112,6 +112,10 @@ struct Staging {
 
 static bool is_fast(const dl_handle* h) { return h->form == DL_FORM_FP32 || h->form == DL_FORM_FP16; }
 
+// a push step leaves phi, u, p stale and the band force and wall reflection of
+// its streaming pending: everything that reads the state settles it first
+static int settled(dl_handle* h) { return (is_fast(h) && h->pushed) ? fast_settle(h) : DL_OK; }
+
 __global__ void f64_to_f32(const double* __restrict__ a, float* __restrict__ b, long long n) {
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (t < n) b[t] = (float)a[t];
@@ -147,6 +151,8 @@ int dl_create(const dl_params* params, int nx, int ny, int nz, int form, dl_hand
     form &= ~DL_SINGLE_PHASE;
     if (form != DL_FORM_FP64 && form != DL_FORM_FP32 && form != DL_FORM_FP16) return DL_ERR_UNSUPPORTED;
     if (single && (params->les != 0 || params->Anu != 0.0)) return DL_ERR_UNSUPPORTED;
+    // the A_nu strain term of geq (program/lbm_drop_xy.f90:461-469) is in the FP64 form only
+    if (form != DL_FORM_FP64 && params->Anu != 0.0) return DL_ERR_UNSUPPORTED;
     if (params->tauf <= 0.5 || params->ds <= 0.0 || params->phi2 == params->phi1) return DL_ERR_ARG;
     if (params->kc < 0 || params->visc_mode < 0 || params->visc_mode > 1) return DL_ERR_ARG;
     dl_handle* h = new (std::nothrow) dl_handle();
@@ -165,6 +171,11 @@ int dl_create(const dl_params* params, int nx, int ny, int nz, int form, dl_hand
     // band forcing: the new u is projected by each block of the fused step
     // after its march ("projection" option; 0: a launch of its own)
     h->proj_in_step = 1;
+    // FP32: the push form where eligible (push_eligible)
+    h->push = (form == DL_FORM_FP32) ? 1 : 0;
+    // push form: staging the next plane in shared memory pays for the single-phase
+    // step (no stencils: little work to hide the loads behind), not the two-phase one
+    h->push_bulk = single ? 1 : 0;
     if (single) {
         // the precursor step: constant nu1, no interface terms
         h->P.kappaf = 0.0;
@@ -245,6 +256,10 @@ int dl_label_droplets(dl_handle* h, int connectivity, int32_t* labels, int64_t* 
                       int64_t max_volumes) {
     if (!h || !ndrops || (max_volumes > 0 && !volumes) || max_volumes < 0) return DL_ERR_ARG;
     if (h->single) return set_error(h, DL_ERR_UNSUPPORTED, "no droplets in the single-phase step");
+    {
+        const int src = settled(h);
+        if (src != DL_OK) return src;
+    }
     long long n = 0;
     int rc = label_droplets(h, connectivity, (int*)labels, &n, volumes, (long long)max_volumes);
     *ndrops = (int64_t)n;
@@ -263,6 +278,10 @@ int dl_save_state(dl_handle* h, void* d_dst) {
     if (!h || !d_dst) return DL_ERR_ARG;
     if (h->form != DL_FORM_FP32 || h->single)
         return set_error(h, DL_ERR_UNSUPPORTED, "device state export is for the two-phase FP32 form");
+    {
+        const int src = settled(h);
+        if (src != DL_OK) return src;
+    }
     const size_t N = h->N;
     float* d = (float*)d_dst;
     DL_CUDA(h, cudaMemcpyAsync(d, h->fs[h->cur], sizeof(float) * Q * N, cudaMemcpyDeviceToDevice, h->stream));
@@ -284,6 +303,7 @@ int dl_load_state(dl_handle* h, const void* d_src) {
                                h->stream));
     h->fields_set = true;
     h->eq_init = true;
+    h->pushed = 0;
     return DL_OK;
 }
 
@@ -299,6 +319,10 @@ int dl_save_adjoint_state(dl_handle* h, void* d_dst) {
     if (!h || !d_dst) return DL_ERR_ARG;
     if (h->form != DL_FORM_FP32 || h->single)
         return set_error(h, DL_ERR_UNSUPPORTED, "device state export is for the two-phase FP32 form");
+    {
+        const int src = settled(h);
+        if (src != DL_OK) return src;
+    }
     const size_t N = h->N;
     float* d = (float*)d_dst;
     DL_CUDA(h, cudaMemcpyAsync(d, h->fs[h->cur], sizeof(float) * Q * N, cudaMemcpyDeviceToDevice, h->stream));
@@ -309,16 +333,28 @@ int dl_save_adjoint_state(dl_handle* h, void* d_dst) {
 
 int dl_adjoint_begin(dl_handle* h, const float* d_dloss_dphi) {
     if (!h || !d_dloss_dphi) return DL_ERR_ARG;
+    {
+        const int src = settled(h);
+        if (src != DL_OK) return src;
+    }
     return adjoint_begin(h, d_dloss_dphi);
 }
 
 int dl_adjoint_step(dl_handle* h, const void* d_state_before, int64_t step) {
     if (!h || !d_state_before || step < 1) return DL_ERR_ARG;
+    {
+        const int src = settled(h);
+        if (src != DL_OK) return src;
+    }
     return adjoint_step(h, (const float*)d_state_before, (long long)step);
 }
 
 int dl_adjoint_init(dl_handle* h, const void* d_state0, float* d_dloss_dphi0) {
     if (!h || !d_state0 || !d_dloss_dphi0) return DL_ERR_ARG;
+    {
+        const int src = settled(h);
+        if (src != DL_OK) return src;
+    }
     return adjoint_init(h, (const float*)d_state0, d_dloss_dphi0);
 }
 
@@ -349,6 +385,16 @@ int dl_set_option(dl_handle* h, const char* key, int64_t value) {
         h->proj_in_step = (int)value;
         return DL_OK;
     }
+    if (strcmp(key, "push") == 0) {
+        if (value < 0 || value > 1) return set_error(h, DL_ERR_ARG, "push must be 0 or 1");
+        h->push = (int)value;
+        return DL_OK;
+    }
+    if (strcmp(key, "stage") == 0) {
+        if (value < 0 || value > 1) return set_error(h, DL_ERR_ARG, "stage must be 0 or 1");
+        h->push_bulk = (int)value;
+        return DL_OK;
+    }
     return set_error(h, DL_ERR_ARG, "unknown option '%s'", key);
 }
 
@@ -368,6 +414,18 @@ int dl_get_option(dl_handle* h, const char* key, int64_t* value) {
     }
     if (strcmp(key, "projection") == 0) {
         *value = h->proj_in_step;
+        return DL_OK;
+    }
+    if (strcmp(key, "push") == 0) {
+        *value = h->push;
+        return DL_OK;
+    }
+    if (strcmp(key, "stage") == 0) {
+        *value = h->push_bulk;
+        return DL_OK;
+    }
+    if (strcmp(key, "pushed") == 0) {  // read only: the state awaits its settle
+        *value = h->pushed;
         return DL_OK;
     }
     return set_error(h, DL_ERR_ARG, "unknown option '%s'", key);
@@ -404,11 +462,16 @@ int dl_set_fields(dl_handle* h, const double* phi, const double* u1, const doubl
     }
     DL_CUDA(h, cudaStreamSynchronize(h->stream));
     h->fields_set = true;
+    h->pushed = 0;
     return DL_OK;
 }
 
 int dl_get_fields(dl_handle* h, double* phi, double* u1, double* u2, double* u3, double* p) {
     if (!h || !phi || !u1 || !u2 || !u3 || !p) return DL_ERR_ARG;
+    {
+        const int src = settled(h);
+        if (src != DL_OK) return src;
+    }
     const size_t N = h->N;
     Staging st;
     const double* d = h->mac64[h->cur];
@@ -434,11 +497,16 @@ int dl_init_equilibrium(dl_handle* h) {
     if (rc != DL_OK) return rc;
     DL_CUDA(h, cudaStreamSynchronize(h->stream));
     h->eq_init = true;
+    h->pushed = 0;
     return DL_OK;
 }
 
 int dl_set_force(dl_handle* h, int mode, const double* fx, const double* fy, const double* fz) {
     if (!h) return DL_ERR_ARG;
+    {
+        const int src = settled(h);
+        if (src != DL_OK) return src;
+    }
     const size_t N = h->N;
     if (mode != DL_FORCE_NONE && mode != DL_FORCE_STATIC && mode != DL_FORCE_SPECTRAL) return DL_ERR_ARG;
     if (mode == DL_FORCE_SPECTRAL && (h->P.kc < 2 || h->sp.K < 1))
@@ -497,7 +565,9 @@ int dl_step(dl_handle* h, int nsteps) {
         int rc = is_fast(h) ? fast_step(h) : fp64_step(h);
         if (rc != DL_OK) return rc;
         if (h->mirror_dev) {
-            DL_LAUNCH(h, false, (mirror_copy<<<1, 32, 0, h->stream>>>(h->d_state, h->mirror_dev, h->step & h->mirror_mask)));
+            // a push step reduces the range of the state it loaded, the previous step's
+            const long long at = h->pushed ? h->step - 1 : h->step;
+            DL_LAUNCH(h, false, (mirror_copy<<<1, 32, 0, h->stream>>>(h->d_state, h->mirror_dev, at & h->mirror_mask)));
             DL_CUDA(h, cudaGetLastError());
         }
     }
@@ -506,6 +576,10 @@ int dl_step(dl_handle* h, int nsteps) {
 
 int dl_get_populations(dl_handle* h, double* f, double* g) {
     if (!h || !f || !g) return DL_ERR_ARG;
+    {
+        const int src = settled(h);
+        if (src != DL_OK) return src;
+    }
     const size_t bytes = Q * h->N * sizeof(double);
     Staging st;
     if (is_fast(h)) {
@@ -570,6 +644,10 @@ int dl_set_populations(dl_handle* h, const double* f, const double* g) {
 
 int dl_set_step(dl_handle* h, int64_t step) {
     if (!h || step < 0) return DL_ERR_ARG;
+    {
+        const int src = settled(h);
+        if (src != DL_OK) return src;
+    }
     h->step = step;
     return DL_OK;
 }
@@ -582,6 +660,10 @@ int dl_get_step(dl_handle* h, int64_t* step) {
 
 int dl_get_minmax(dl_handle* h, double* mn, double* mx) {
     if (!h || !mn || !mx) return DL_ERR_ARG;
+    {
+        const int src = settled(h);
+        if (src != DL_OK) return src;
+    }
     double v[2];
     DL_CUDA(h, cudaMemcpyAsync(v, h->d_state, sizeof(v), cudaMemcpyDeviceToHost, h->stream));
     DL_CUDA(h, cudaStreamSynchronize(h->stream));
@@ -592,6 +674,10 @@ int dl_get_minmax(dl_handle* h, double* mn, double* mx) {
 
 int dl_get_minmax_async(dl_handle* h, double* dst) {
     if (!h || !dst) return DL_ERR_ARG;
+    {
+        const int src = settled(h);
+        if (src != DL_OK) return src;
+    }
     // phi_min and phi_max are the first two fields of the device state
     DL_CUDA(h, cudaMemcpyAsync(dst, h->d_state, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     return DL_OK;
@@ -642,6 +728,7 @@ int dl_sync(dl_handle* h) {
     DL_CUDA(h, cudaStreamSynchronize(h->stream));
     DevState s;
     DL_CUDA(h, cudaMemcpy(&s, h->d_state, sizeof(s), cudaMemcpyDeviceToHost));
+    if (s.wait_timeout) return set_error(h, DL_ERR_TIMEOUT, "a step kernel's wait for its staged populations gave up");
     if (s.nan_flag) return set_error(h, DL_ERR_NAN, "non-finite phi/u/p first seen at step %lld", s.nan_step);
     return DL_OK;
 }
@@ -649,6 +736,10 @@ int dl_sync(dl_handle* h) {
 int dl_energy(dl_handle* h, dl_energy_diag* out, double* spectrum, int64_t nbins) {
     if (!h || !out) return DL_ERR_ARG;
     if (!h->fields_set) return set_error(h, DL_ERR_STATE, "dl_energy before dl_set_fields");
+    {
+        const int src = settled(h);
+        if (src != DL_OK) return src;
+    }
     return energy_diagnostics(h, out, spectrum, (long long)nbins);
 }
 
@@ -664,6 +755,10 @@ int dl_fp64_ceiling(dl_handle* h, double* tflops) {
 
 int dl_reduce(dl_handle* h, dl_diag* out) {
     if (!h || !out) return DL_ERR_ARG;
+    {
+        const int src = settled(h);
+        if (src != DL_OK) return src;
+    }
     int rc = is_fast(h) ? reduce_fields_f32(h, h->mac32[h->cur], out) : reduce_fields(h, h->mac64[h->cur], out);
     if (rc != DL_OK) return rc;
     DevState s;

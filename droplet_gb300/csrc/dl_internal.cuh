@@ -46,7 +46,7 @@ struct DevState {
     int nan_flag;                    // nonzero once a non-finite value was produced
     long long nan_step;              // step at which it was first seen
     int quirk_scans;                 // number of exact serial-order min scans taken
-    int pad_;
+    int wait_timeout;                // a bounded wait in a step kernel gave up (the step's values are void)
     // spectral forcing
     double sp_energy;                // band energy of the last forcing evaluation
     double sp_coef;                  // 0.5 eps / E
@@ -143,6 +143,9 @@ struct dl_handle {
     int l2_prefetch;         // fused kernel: bulk L2 prefetch of the next plane's pulls
     int sp_pipeline;         // single-phase kernel: next plane's pulls held in registers
     int proj_in_step;        // band forcing: projection of the new u inside the fused step (else its own launch)
+    int push;                // FP32: step in the push form where eligible (option "push")
+    int pushed;              // the state is a push step's: fields stale, band force and wall reflection pending
+    int push_bulk;           // push form, full tiles: next plane staged by bulk copies (option "stage")
     double* mirror_dev;      // dl_set_minmax_mirror: device address of the host mirror (or null)
     long long mirror_mask;   // its slots - 1 (slots a power of two)
     // dl_energy: cuFFT plan and buffers (allocated on first use)
@@ -199,6 +202,10 @@ int fast_init_equilibrium(dl_handle* h);
 int fast_get_populations(dl_handle* h, double* d_f, double* d_g);
 int fast_set_populations(dl_handle* h, const double* d_f, const double* d_g);
 int fast_step(dl_handle* h);
+// push form (step_push.cu)
+bool push_eligible(const dl_handle* h);
+int push_step(dl_handle* h);
+int fast_settle(dl_handle* h);  // complete a push step's state (no-op when settled)
 int fast_prepare_force(dl_handle* h, int mode);
 int spectral_project_f32(dl_handle* h, const float* d_u1, const float* d_u2, const float* d_u3);
 // batched ensembles of fast-form handles (step_fast.cu)

@@ -265,6 +265,11 @@ extern "C" int dl_reduce_static(dl_handle* h, int nblocks, dl_diag* out) {
                              nblocks, DL_REDUCE_STATIC_MAX_BLOCKS, (int)DL_REDUCE_STATIC_SCRATCH_BYTES,
                              DL_REDUCE_STATIC_MAX_BLOCKS, dl::RS_DEFAULT_BLOCKS);
     if (!h->fields_set) return dl::set_error(h, DL_ERR_STATE, "dl_reduce_static: fields not set");
+    // a push step's state is settled first (one launch, no allocation)
+    if ((h->form == DL_FORM_FP32 || h->form == DL_FORM_FP16) && h->pushed) {
+        const int src = dl::fast_settle(h);
+        if (src != DL_OK) return src;
+    }
     int prev = -1;
     if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
     if (prev != h->device) {

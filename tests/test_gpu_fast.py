@@ -190,6 +190,7 @@ def test_projection_in_step_equals_own_launch(form, tol_phi, tol_u, shape, lz):
     out = {}
     for proj in (0, 1):
         g = Droplet(P, shape, form)
+        g.set_option("push", 0)  # the projection options are the pull form's
         g.set_option("projection", proj)
         if lz:
             g.set_option("lz", lz)
@@ -200,12 +201,13 @@ def test_projection_in_step_equals_own_launch(form, tol_phi, tol_u, shape, lz):
     assert e["phi"] <= tol_phi and e["u"] <= tol_u and e["p"] <= tol_u, e
 
 
-@pytest.mark.parametrize("form", [FORM_FP64, FORM_FP32, FORM_FP16])
-def test_minmax_mirror_holds_every_step(form):
-    """dl_set_minmax_mirror: the step that takes the counter to n writes its
-    phi range into slot n % nslots of the pinned mirror, the values that
-    dl_get_minmax returns after it; off again, the steps write nothing; memory
-    that is not page-locked is refused on the host."""
+@pytest.mark.parametrize("form,push", [(FORM_FP64, 0), (FORM_FP32, 0), (FORM_FP32, 1), (FORM_FP16, 0)])
+def test_minmax_mirror_holds_every_step(form, push):
+    """dl_set_minmax_mirror: the step that takes the counter to n writes the
+    phi range of step n into slot n % nslots of the pinned mirror (the push
+    form: the range of step n-1, the state it loaded, into slot n-1), the
+    values that dl_get_minmax returns for that state; off again, the steps
+    write nothing; memory that is not page-locked is refused on the host."""
     import torch
 
     from droplet_gb300 import DropletError
@@ -213,13 +215,21 @@ def test_minmax_mirror_holds_every_step(form):
     shape = (24, 20, 16)
     P, f, mode, force = make_case("plain", shape)
     g = Droplet(P, shape, form)
+    if form == FORM_FP32:
+        g.set_option("push", push)
     start(g, f, mode, force)
     buf = torch.full((4, 2), -1.0, dtype=torch.float64).pin_memory()
     g.set_minmax_mirror(buf.data_ptr(), 4)
     for n in range(1, 10):
+        before = g.minmax()  # the range of step n-1 (settles a push step's state)
         g.step(1)
         g.sync()
-        assert (float(buf[n % 4, 0]), float(buf[n % 4, 1])) == g.minmax(), n
+        if push:
+            # (before the first step the range is init's (phi1, phi2), not a computed one)
+            if n > 1:
+                assert (float(buf[(n - 1) % 4, 0]), float(buf[(n - 1) % 4, 1])) == before, n
+        else:
+            assert (float(buf[n % 4, 0]), float(buf[n % 4, 1])) == g.minmax(), n
     with pytest.raises(DropletError):
         g.set_minmax_mirror(buf.data_ptr(), 3)  # not a power of two
     g.set_minmax_mirror(0)
