@@ -522,10 +522,12 @@ def run_ours(args):
     avg_main_ms = prof["main_ms"] / max(prof["main_launches"], 1)
     bytes_per_launch = bytes_per_site(form, w.single_phase) * N
     achieved = bytes_per_launch / (avg_main_ms / 1e3) / 1e9
-    traffic = committed_traffic(f"{MAIN_KERNEL[form]}_{args.form}", w.name)
+    # the FP32 form steps in the push form where eligible (its own kernel)
+    kname = "step_push" if (form != 64 and sim.get_option("pushed")) else MAIN_KERNEL[form]
+    traffic = committed_traffic(f"{kname}_{args.form}", w.name)
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_kind,
-                "kernel": MAIN_KERNEL[form], "kernel_ms": round(avg_main_ms, 5),
+                "kernel": kname, "kernel_ms": round(avg_main_ms, 5),
                 "kernel_share": round(prof["main_ms"] / max(prof["total_ms"], 1e-12), 4),
                 "timed_launches": int(prof["timed_launches"]), "event_stride": stride,
                 "algorithmic_bytes_per_launch": bytes_per_launch}
@@ -566,7 +568,7 @@ def run_ours(args):
         sim2 = Droplet(w.params, w.shape, w.form, single_phase=w.single_phase)
         sim2.set_stream(stream.cuda_stream)
         if tune is not None:
-            for k in ("lz", "prefetch", "pipeline"):
+            for k in ("lz", "prefetch", "pipeline", "stage"):
                 if k in tune:
                     sim2.set_option(k, tune[k])
         torch.cuda.synchronize()
@@ -733,7 +735,7 @@ def measure_ensemble(n_members: int, steps: int, form: int, stream, tune: bool =
         d.set_fields(**w.fields)
         d.init_equilibrium()
         d.set_force(w.force_mode)
-        d.set_option("lz", tuned["lz"])
+        d.set_option("lz", min(tuned["lz"], w.shape[2]))
         d.step(2)
         solos.append(d)
     torch.cuda.synchronize()

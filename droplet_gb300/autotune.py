@@ -19,7 +19,7 @@ import json
 import os
 import threading
 
-LZ_CANDIDATES = (4, 8, 16, 32)
+LZ_CANDIDATES = (4, 8, 16, 32, 64)
 BPS_CANDIDATES = (1, 2)
 _lock = threading.Lock()
 
@@ -75,13 +75,21 @@ def _key(kind: str, form: int, shapes, extra: str) -> str:
 
 
 def tune_droplet(sim, steps: int = 20, use_cache: bool = True) -> dict:
-    """Pick "lz" and "prefetch" (and, for the single-phase step, "pipeline")
-    for one Droplet (fast forms). Returns the chosen settings."""
+    """Pick "lz" and, for the push form, "stage", else "prefetch" (and, for
+    the single-phase pull step, "pipeline") for one Droplet (fast forms).
+    Returns the chosen settings."""
     p = sim.params
     single = bool(getattr(sim, "single_phase", False))
+    # the push form (FP32 where eligible) has its own knob, the staging of the
+    # next plane in shared memory; the pull form the L2 prefetch (and, single
+    # phase, the register pipeline)
+    push = bool(sim.get_option("push_eligible"))
     key = _key("single", sim.form, [(sim.nx, sim.ny, sim.nz)],
-               f"les{int(bool(p.les))}" + ("_1phase" if single else "") + "_pf")
-    knobs = ["prefetch"] + (["pipeline"] if single else [])
+               f"les{int(bool(p.les))}" + ("_1phase" if single else "") + ("_push" if push else "_pf"))
+    if push:
+        knobs = ["stage"]
+    else:
+        knobs = ["prefetch"] + (["pipeline"] if single else [])
     if use_cache:
         hit = _load().get(key)
         if hit:

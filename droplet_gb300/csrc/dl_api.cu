@@ -424,6 +424,10 @@ int dl_get_option(dl_handle* h, const char* key, int64_t* value) {
         *value = h->push_bulk;
         return DL_OK;
     }
+    if (strcmp(key, "push_eligible") == 0) {  // read only: the next step takes the push form
+        *value = (h->form == DL_FORM_FP32 && push_eligible(h)) ? 1 : 0;
+        return DL_OK;
+    }
     if (strcmp(key, "pushed") == 0) {  // read only: the state awaits its settle
         *value = h->pushed;
         return DL_OK;
@@ -728,7 +732,6 @@ int dl_sync(dl_handle* h) {
     DL_CUDA(h, cudaStreamSynchronize(h->stream));
     DevState s;
     DL_CUDA(h, cudaMemcpy(&s, h->d_state, sizeof(s), cudaMemcpyDeviceToHost));
-    if (s.wait_timeout) return set_error(h, DL_ERR_TIMEOUT, "a step kernel's wait for its staged populations gave up");
     if (s.nan_flag) return set_error(h, DL_ERR_NAN, "non-finite phi/u/p first seen at step %lld", s.nan_step);
     return DL_OK;
 }

@@ -46,7 +46,7 @@ struct DevState {
     int nan_flag;                    // nonzero once a non-finite value was produced
     long long nan_step;              // step at which it was first seen
     int quirk_scans;                 // number of exact serial-order min scans taken
-    int wait_timeout;                // a bounded wait in a step kernel gave up (the step's values are void)
+    int pad_;
     // spectral forcing
     double sp_energy;                // band energy of the last forcing evaluation
     double sp_coef;                  // 0.5 eps / E

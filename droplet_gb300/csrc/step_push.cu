@@ -57,11 +57,6 @@ __device__ __forceinline__ void cp_async4(float* smem_dst, const float* gmem_src
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
-// bulk prefetch of [p, p + bytes) into L2 (16-byte aligned, bytes a multiple of 16)
-__device__ __forceinline__ void prefetch_rows_l2(const void* p, unsigned bytes) {
-    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;\n" ::"l"(p), "r"(bytes) : "memory");
-}
-
 struct PushArgs {
     FastArgs a;
     int pending;           // the loaded populations lack the band force and wall reflection of their streaming
@@ -261,29 +256,30 @@ __device__ __forceinline__ void collide_push(const PushArgs& pa, int t, const fl
     }
 
     // ---- collision, each direction with its opposite, pushed at once ----
-    // f: df* = (1 - wf) df + wf dfeq, dfeq_i = [i=0] dphi + F_i dA + E_i (3 phi c.u + kf (4.5 (c.gphi)^2 - |c|^2 gq))
-    // g: dg* = (1 - wg) dg + wg dgeq + 3 E_i c.F, dgeq_i = E_i (S + 3 c.u + 4.5 (c.u)^2 + kg (4.5 (c.gphi)^2 - |c|^2 gq))
-    const float wf = a.omf, wf1 = 1.f - wf, wg = omg, wg1 = 1.f - omg;
+    // f: df* = df + wf (dfeq - df), dfeq_i = [i=0] dphi + F_i dA + E_i (3 phi c.u + kf (4.5 (c.gphi)^2 - |c|^2 gq))
+    // g: dg* = dg + wg (dgeq - dg) + 3 E_i c.F, dgeq_i = E_i (S + 3 c.u + 4.5 (c.u)^2 + kg (4.5 (c.gphi)^2 - |c|^2 gq))
+    // (the relaxation acts on the small non-equilibrium part eq - v, as fg_cal's
+    // f - (f - feq)/tau does, not on two large terms of opposite sign)
+    const float wf = a.omf, wg = omg;
     float* fo = (float*)a.fo;
     float* go = (float*)a.go;
     // destination index of direction i (x + c_i, wrapped)
     auto dst = [&](int i) -> unsigned { return (unsigned)i * N + zo[1 + cz(i)] + yr[1 + cy(i)] + xs[1 + cx(i)]; };
-    if (!SP) fo[dst(0)] = fmaf(wf1, v[0], wf * (dphi + Fw(0) * dA));
-    go[dst(0)] = fmaf(wg1, v[Q], wg * (Ew(0) * S));
-    // per class (1 axis, 2 diagonal): even parts and odd coefficients
-    float Kf[3] = {0.f, 0.f, 0.f}, Bf[3] = {0.f, 0.f, 0.f}, Af[3] = {0.f, 0.f, 0.f}, Kg[3], Bg[3], Ag[3];
+    if (!SP) fo[dst(0)] = fmaf(wf, (dphi + Fw(0) * dA) - v[0], v[0]);
+    go[dst(0)] = fmaf(wg, Ew(0) * S - v[Q], v[Q]);
+    // per class (1 axis, 2 diagonal): even parts and odd coefficients of the equilibria
+    float Kf[3] = {0.f, 0.f, 0.f}, Bf[3] = {0.f, 0.f, 0.f}, Af[3] = {0.f, 0.f, 0.f}, Kg[3], Ag[3];
 #pragma unroll
     for (int c = 1; c <= 2; ++c) {
         const int i = c == 1 ? 1 : 7;
         const float E = Ew(i);
         if (!SP) {
-            Kf[c] = wf * (Fw(i) * dA - E * c2w(i) * a.kf * gq);
-            Bf[c] = wf * (3.f * E) * phi;
-            Af[c] = wf * (4.5f * E) * a.kf;
+            Kf[c] = Fw(i) * dA - E * c2w(i) * a.kf * gq;
+            Bf[c] = (3.f * E) * phi;
+            Af[c] = (4.5f * E) * a.kf;
         }
-        Kg[c] = wg * (E * (S - c2w(i) * a.kg * gq));
-        Bg[c] = wg * (3.f * E);
-        Ag[c] = wg * (4.5f * E);
+        Kg[c] = E * (S - c2w(i) * a.kg * gq);
+        Ag[c] = 4.5f * E;
     }
     // c . v for the representatives 1, 2, 3 (axes) and 7, 8, 9, 10 (diagonals)
     const float uxy = u1 + u2, uxmy = u1 - u2;
@@ -304,22 +300,23 @@ __device__ __forceinline__ void collide_push(const PushArgs& pa, int t, const fl
     auto pairc = [&](int i, int j, int c) {
         const float cu = dotc(i, u1, u2, u3, uxy, uxmy);
         const float e3 = 3.f * Ew(i);
-        float gd = Bg[c] * cu;
-        if (FMODE == F_ARRAY) gd = fmaf(e3, dotc(i, Fx, Fy, Fz, Fxy, Fxmy), gd);
+        const float gd = e3 * cu;  // odd part of geq
+        float fF = 0.f;            // the force term, odd
+        if (FMODE == F_ARRAY) fF = e3 * dotc(i, Fx, Fy, Fz, Fxy, Fxmy);
         float ge;
         if (!SP) {
             const float cg = dotc(i, gx, gy, gz, gxy, gxmy);
             const float t = cg * cg;
             const float fe = fmaf(Af[c], t, Kf[c]);
             const float fd = Bf[c] * cu;
-            fo[dst(i)] = fmaf(wf1, v[i], fe + fd);
-            fo[dst(j)] = fmaf(wf1, v[j], fe - fd);
+            fo[dst(i)] = fmaf(wf, (fe + fd) - v[i], v[i]);
+            fo[dst(j)] = fmaf(wf, (fe - fd) - v[j], v[j]);
             ge = fmaf(Ag[c], fmaf(a.kg, t, cu * cu), Kg[c]);
         } else {
             ge = fmaf(Ag[c], cu * cu, Kg[c]);
         }
-        go[dst(i)] = fmaf(wg1, v[Q + i], ge + gd);
-        go[dst(j)] = fmaf(wg1, v[Q + j], ge - gd);
+        go[dst(i)] = fmaf(wg, (ge + gd) - v[Q + i], v[Q + i]) + fF;
+        go[dst(j)] = fmaf(wg, (ge - gd) - v[Q + j], v[Q + j]) - fF;
     };
     pairc(1, 4, 1);
     pairc(2, 5, 1);
@@ -686,30 +683,6 @@ __device__ __forceinline__ void push_body(const PushArgs& pa, float* smem) {
         }
         cp_async_commit();
     };
-    // L2 prefetch of plane zp's rows of every population array that this block
-    // loads (rows y0-1 .. y0+TY, columns x0-1 .. x0+TX, clipped to the row):
-    // the loads issued for that plane later find them in L2
-    auto plane_prefetch = [&](int zp) {
-        constexpr int NARR = SP ? 1 : 2;
-        constexpr int NROW = SP ? TY : EY1;
-        const int xa = max(x0 - (SP ? 0 : 1), 0), xb = min(x0 + TX + (SP ? 0 : 1), nx);
-        const size_t zo = (size_t)wrap_near(zp, nz) * nxy;
-        const size_t arr_end = ((size_t)Q * N * sizeof(float)) & ~(size_t)15;
-        for (int t = tid; t < NARR * Q * NROW; t += NT) {
-            const int r = t % NROW, q = t / NROW, i = q % Q;
-            const bool isg = SP || q >= Q;
-            const int yy = SP ? y0 + r : y0 - 1 + r;
-            if (SP && yy >= ny) continue;
-            const char* base = (const char*)(isg ? a.g : a.f);
-            const size_t row = (size_t)i * N + zo + (size_t)nx * (unsigned)pmod(yy, ny);
-            size_t b0 = (row + (size_t)xa) * sizeof(float), b1 = (row + (size_t)xb) * sizeof(float);
-            b0 &= ~(size_t)15;
-            b1 = (b1 + 15) & ~(size_t)15;
-            if (b1 > arr_end) b1 = arr_end;
-            if (b1 > b0) prefetch_rows_l2(base + b0, (unsigned)(b1 - b0));
-        }
-    };
-
     // the halo site's moments of plane zp into the ring, streamed pair by pair
     // from shared memory (band force of the sources, wall reflection, sums)
     auto halo_plane = [&](int zp) {
@@ -777,10 +750,6 @@ __device__ __forceinline__ void push_body(const PushArgs& pa, float* smem) {
         float A[2 * Q], B[2 * Q];
         float oA[5], oB[5];  // own moments (dphi, u1, u2, u3, dp) of the planes held in A, B
         // planes zlo (= z0 - 1, moments only) and z0
-        if (a.l2_prefetch) {
-            plane_prefetch(z0 + 1);
-            if (z0 + 2 <= z1) plane_prefetch(z0 + 2);
-        }
         if (BULK) {
             bulk_issue(z0 - 1);
             issue_halo(z0 - 1);
@@ -833,7 +802,6 @@ __device__ __forceinline__ void push_body(const PushArgs& pa, float* smem) {
             }
             // the force of plane t+4, read from iteration t+2 on (after the next barrier)
             if (fpend && t + 4 <= z1 + 1) fsynth(t + 4);
-            if (a.l2_prefetch && t + 3 <= z1) plane_prefetch(t + 3);
             if (act) {
                 const float4* mc = s_mom + (t & (PSL - 1)) * P1;
                 const float4* ml = s_mom + ((t - 1) & (PSL - 1)) * P1;

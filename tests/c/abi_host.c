@@ -70,17 +70,28 @@ int main(int argc, char** argv) {
     check(h, dl_set_fields(h, f[0], f[1], f[2], f[3], f[4]), "dl_set_fields");
     check(h, dl_init_equilibrium(h), "dl_init_equilibrium");
     /* every step's phi range in a page-locked mirror of 2 slots, checked
-     * against dl_get_minmax after each step */
+     * against dl_get_minmax: the pull form writes step k's range into slot
+     * k % 2; the push form (FP32) writes the range of the state a step
+     * loads, step k-1's, into slot (k-1) % 2 */
     double* mirror = NULL;
     check(h, dl_host_alloc(4 * sizeof(double), (void**)&mirror), "dl_host_alloc");
     check(h, dl_set_minmax_mirror(h, mirror, 2), "dl_set_minmax_mirror");
+    int64_t push = 0;
+    check(h, dl_get_option(h, "push_eligible", &push), "dl_get_option");
     int mismatches = 0;
     for (int k = 1; k <= steps; ++k) {
+        double mn0, mx0;
+        check(h, dl_get_minmax(h, &mn0, &mx0), "dl_get_minmax");
         check(h, dl_step(h, 1), "dl_step");
         check(h, dl_sync(h), "dl_sync");
         double mn, mx;
         check(h, dl_get_minmax(h, &mn, &mx), "dl_get_minmax");
-        if (mirror[2 * (k % 2)] != mn || mirror[2 * (k % 2) + 1] != mx) ++mismatches;
+        if (push) {
+            /* before the first step the range is init's (phi1, phi2), not a computed one */
+            if (k > 1 && (mirror[2 * ((k - 1) % 2)] != mn0 || mirror[2 * ((k - 1) % 2) + 1] != mx0)) ++mismatches;
+        } else if (mirror[2 * (k % 2)] != mn || mirror[2 * (k % 2) + 1] != mx) {
+            ++mismatches;
+        }
     }
     check(h, dl_set_minmax_mirror(h, NULL, 0), "dl_set_minmax_mirror");
     check(h, dl_host_free(mirror), "dl_host_free");

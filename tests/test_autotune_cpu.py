@@ -23,6 +23,10 @@ class FakeSim:
         assert k in ("lz", "prefetch")
         setattr(self, k, v)
 
+    def get_option(self, k):
+        assert k == "push_eligible"
+        return 0
+
     def step(self, n):
         self.steps += n
 
@@ -44,6 +48,34 @@ def test_tuner_picks_fastest_and_caches(tmp_path, monkeypatch):
     sim2 = FakeSim()
     r2 = autotune.tune_droplet(sim2, steps=5)
     assert r2["cached"] and sim2.lz == 8 and sim2.prefetch == 1 and sim2.steps == 0
+
+
+class FakePushSim(FakeSim):
+    """A handle that steps in the push form: its knob is "stage" (lz = 16 with
+    staging fastest); "prefetch" is never set."""
+
+    def __init__(self):
+        super().__init__()
+        self.stage = 0
+
+    def set_option(self, k, v):
+        assert k in ("lz", "stage")
+        setattr(self, k, v)
+
+    def get_option(self, k):
+        assert k == "push_eligible"
+        return 1
+
+    def profile_read(self):
+        return {"main_ms": self.steps * (1.0 + abs(self.lz - 16) / 16.0 - 0.1 * self.stage)}
+
+
+def test_tuner_push_form_tunes_staging(tmp_path, monkeypatch):
+    monkeypatch.setenv("DROPLET_GB300_TUNE_CACHE", str(tmp_path / "tune.json"))
+    monkeypatch.setattr(autotune, "gpu_name", lambda: "fake-gpu")
+    sim = FakePushSim()
+    r = autotune.tune_droplet(sim, steps=5)
+    assert r["lz"] == 16 and r["stage"] == 1 and "prefetch" not in r and sim.stage == 1
 
 
 class FakeEnsemble:

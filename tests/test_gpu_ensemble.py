@@ -52,6 +52,8 @@ def test_ensemble_matches_members_stepped_alone(form, persistent, spectral, les,
     for m, (mem, (P, f)) in enumerate(zip(ens.members, cases)):
         solo = Droplet(P, SHAPES[m], form)
         solo.set_option("lz", 8)
+        if persistent and form == FORM_FP32:
+            solo.set_option("push", 0)  # the persistent launch steps the pull form
         start(solo, f, spectral)
         solo.step(steps)
         a, b = mem.get_fields(), solo.get_fields()

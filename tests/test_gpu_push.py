@@ -144,3 +144,18 @@ def test_staged_planes_equal_loaded_planes(case):
     for k in out[0][0]:
         assert np.array_equal(out[0][0][k], out[1][0][k]), k
     assert np.array_equal(out[0][1][0], out[1][1][0]) and np.array_equal(out[0][1][1], out[1][1][1])
+
+
+def test_push_bitwise_independent_of_z_chunks():
+    """Without band forcing (no FP64 atomics in the step) the push form gives
+    the same bits whatever the z chunk of a block: every site's loads,
+    moments and collision are the same arithmetic in every block that takes
+    them (the ring sites are computed again by each neighbouring block)."""
+    shape = (40, 24, 30)
+    P, f, mode, force = make_case("les_static_force", shape)
+    out = []
+    for lz in (4, 7, 30):
+        g = run(P, f, mode, force, shape, 12, 1, lz)
+        out.append(g.get_fields())
+    for k in out[0]:
+        assert np.array_equal(out[0][k], out[1][k]) and np.array_equal(out[0][k], out[2][k]), k
