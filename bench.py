@@ -586,12 +586,14 @@ def run_ours(args):
         sim2.set_minmax_mirror(slots.data_ptr(), 2)
         done = [torch.cuda.Event(), torch.cuda.Event()]
         seen = []
+        # the push form's launch n writes step n-1's range (the state it loads) into slot n-1
+        lag = 1 if sim2.get_option("push_eligible") else 0
         for k in range(k_e2e):
             sim2.step(1)
             done[k % 2].record(stream)
             if k > 0:
                 done[(k - 1) % 2].synchronize()
-                seen.append(float(slots[k % 2, 1]))
+                seen.append(float(slots[(k - lag) % 2, 1]))
             if (k + 1) % args.diag_every == 0 or k + 1 == k_e2e:
                 sim2.reduce()  # device -> host read of the whole-domain diagnostics
                 n_full += 1
@@ -599,7 +601,7 @@ def run_ours(args):
                 sim2.get_fields_into(out)  # the periodic field output (D2H)
                 n_out += 1
         done[(k_e2e - 1) % 2].synchronize()
-        seen.append(float(slots[k_e2e % 2, 1]))
+        seen.append(float(slots[(k_e2e - lag) % 2, 1]))
         assert len(seen) == k_e2e
         sim2.get_fields_into(out)
         n_out += 1
