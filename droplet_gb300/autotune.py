@@ -1,8 +1,10 @@
 """Autotuner for the launch shape of the fused step.
 
 The tunable knobs are those of the C-ABI: for one domain the number of z
-planes a block marches ("lz", ``dl_set_option``), the bulk L2 prefetch
-("prefetch") and, for the single-phase step, "pipeline"; for an ensemble "lz"
+planes a block marches ("lz", ``dl_set_option``) and, in the push form, the
+staging of the next plane ("stage" 0, 1, and 2 on full 32 x 8 tiles), in the
+pull form the bulk L2 prefetch ("prefetch") and, for the single-phase step,
+"pipeline"; for an ensemble "lz"
 and, with its persistent launch, the number of blocks per SM
 ("blocks_per_sm", ``dl_batch_set_option``). Each candidate is timed after a
 few warm-up steps, with the library's own per-launch CUDA events (one domain,
@@ -86,8 +88,12 @@ def tune_droplet(sim, steps: int = 20, use_cache: bool = True) -> dict:
     push = bool(sim.get_option("push_eligible"))
     key = _key("single", sim.form, [(sim.nx, sim.ny, sim.nz)],
                f"les{int(bool(p.les))}" + ("_1phase" if single else "") + ("_push" if push else "_pf"))
+    values = {"prefetch": (0, 1), "pipeline": (0, 1), "stage": (0, 1)}
     if push:
         knobs = ["stage"]
+        # stage 2 (tensor copies) needs full 32 x 8 tiles
+        if sim.nx % 32 == 0 and sim.ny % 8 == 0:
+            values["stage"] = (0, 1, 2)
     else:
         knobs = ["prefetch"] + (["pipeline"] if single else [])
     if use_cache:
@@ -99,7 +105,7 @@ def tune_droplet(sim, steps: int = 20, use_cache: bool = True) -> dict:
             return dict(hit, cached=True)
     best = None
     timings = {}
-    combos = [dict(zip(knobs, v)) for v in itertools.product((0, 1), repeat=len(knobs))]
+    combos = [dict(zip(knobs, v)) for v in itertools.product(*(values[k] for k in knobs))]
     for combo in combos:
         for k, v in combo.items():
             sim.set_option(k, v)

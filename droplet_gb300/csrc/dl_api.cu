@@ -176,6 +176,7 @@ int dl_create(const dl_params* params, int nx, int ny, int nz, int form, dl_hand
     // push form: staging the next plane in shared memory pays for the single-phase
     // step (no stencils: little work to hide the loads behind), not the two-phase one
     h->push_bulk = single ? 1 : 0;
+    h->push_wait_ns = 2000000000LL;
     if (single) {
         // the precursor step: constant nu1, no interface terms
         h->P.kappaf = 0.0;
@@ -391,8 +392,20 @@ int dl_set_option(dl_handle* h, const char* key, int64_t value) {
         return DL_OK;
     }
     if (strcmp(key, "stage") == 0) {
-        if (value < 0 || value > 1) return set_error(h, DL_ERR_ARG, "stage must be 0 or 1");
+        if (value < 0 || value > 2) return set_error(h, DL_ERR_ARG, "stage must be 0, 1 or 2");
+        if (value == 2 && !push_tma_eligible(h))
+            return set_error(h, DL_ERR_UNSUPPORTED, "stage 2 (tensor copies) needs nx a multiple of 32 and ny of 8");
         h->push_bulk = (int)value;
+        return DL_OK;
+    }
+    if (strcmp(key, "wait_ns") == 0) {
+        if (value < 1000 || value > 60000000000LL) return set_error(h, DL_ERR_ARG, "wait_ns must be in [1e3, 6e10]");
+        h->push_wait_ns = value;
+        return DL_OK;
+    }
+    if (strcmp(key, "stage_extra_tx") == 0) {
+        if (value < 0 || value > 4096 || value % 16) return set_error(h, DL_ERR_ARG, "stage_extra_tx must be 0 .. 4096, a multiple of 16");
+        h->push_extra_tx = (int)value;
         return DL_OK;
     }
     return set_error(h, DL_ERR_ARG, "unknown option '%s'", key);
@@ -422,6 +435,14 @@ int dl_get_option(dl_handle* h, const char* key, int64_t* value) {
     }
     if (strcmp(key, "stage") == 0) {
         *value = h->push_bulk;
+        return DL_OK;
+    }
+    if (strcmp(key, "wait_ns") == 0) {
+        *value = h->push_wait_ns;
+        return DL_OK;
+    }
+    if (strcmp(key, "stage_extra_tx") == 0) {
+        *value = h->push_extra_tx;
         return DL_OK;
     }
     if (strcmp(key, "push_eligible") == 0) {  // read only: the next step takes the push form
@@ -732,6 +753,7 @@ int dl_sync(dl_handle* h) {
     DL_CUDA(h, cudaStreamSynchronize(h->stream));
     DevState s;
     DL_CUDA(h, cudaMemcpy(&s, h->d_state, sizeof(s), cudaMemcpyDeviceToHost));
+    if (s.wait_timeout) return set_error(h, DL_ERR_TIMEOUT, "a tensor copy of the staged plane did not complete in time");
     if (s.nan_flag) return set_error(h, DL_ERR_NAN, "non-finite phi/u/p first seen at step %lld", s.nan_step);
     return DL_OK;
 }

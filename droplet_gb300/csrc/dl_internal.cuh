@@ -46,7 +46,7 @@ struct DevState {
     int nan_flag;                    // nonzero once a non-finite value was produced
     long long nan_step;              // step at which it was first seen
     int quirk_scans;                 // number of exact serial-order min scans taken
-    int pad_;
+    int wait_timeout;                // nonzero once a bounded device-side wait ran out
     // spectral forcing
     double sp_energy;                // band energy of the last forcing evaluation
     double sp_coef;                  // 0.5 eps / E
@@ -145,7 +145,12 @@ struct dl_handle {
     int proj_in_step;        // band forcing: projection of the new u inside the fused step (else its own launch)
     int push;                // FP32: step in the push form where eligible (option "push")
     int pushed;              // the state is a push step's: fields stale, band force and wall reflection pending
-    int push_bulk;           // push form, full tiles: next plane staged by bulk copies (option "stage")
+    int push_bulk;           // push form: next plane staged in shared memory (option "stage": 0 registers,
+                             // 1 per-thread asynchronous copies, 2 tensor copies, full tiles only)
+    unsigned char push_tmap[4][128];  // stage 2: tensor maps of fs[0], fs[1], gs[0], gs[1]
+    int push_tmap_ok;
+    long long push_wait_ns;  // stage 2: limit of a block's wait for its staged plane (option "wait_ns")
+    int push_extra_tx;       // stage 2, tests of that limit: bytes expected beyond the copies' ("stage_extra_tx")
     double* mirror_dev;      // dl_set_minmax_mirror: device address of the host mirror (or null)
     long long mirror_mask;   // its slots - 1 (slots a power of two)
     // dl_energy: cuFFT plan and buffers (allocated on first use)
@@ -203,6 +208,7 @@ int fast_get_populations(dl_handle* h, double* d_f, double* d_g);
 int fast_set_populations(dl_handle* h, const double* d_f, const double* d_g);
 int fast_step(dl_handle* h);
 // push form (step_push.cu)
+bool push_tma_eligible(const dl_handle* h);
 bool push_eligible(const dl_handle* h);
 int push_step(dl_handle* h);
 int fast_settle(dl_handle* h);  // complete a push step's state (no-op when settled)

@@ -1038,6 +1038,7 @@ void fast_free(dl_handle* h) {
         h->fs[k] = h->gs[k] = nullptr;
         h->mac32[k] = nullptr;
     }
+    h->push_tmap_ok = 0;  // the tensor maps name the freed buffers
     cudaFree(h->force32);
     h->force32 = nullptr;
     fast_spectral_free(h);

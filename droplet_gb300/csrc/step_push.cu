@@ -34,14 +34,19 @@
 // Per block: a 32 x 8 tile of columns marching up z. Every plane's moments
 // (dphi, u) of the tile and a one-cell ring around it go to a four-slot ring
 // in shared memory; with a pending band force, the force of a two-cell ring
-// is synthesised per plane into a four-slot ring (Fx, Fy, Fz and c.F of the
-// four body diagonals). One barrier per plane. The populations of plane z+1
-// are loaded while plane z is collided.
+// is synthesised per plane into a four-slot ring (Fx, Fy, Fz). One barrier
+// per plane. The populations of plane z+1 are loaded while plane z is
+// collided: into registers (option "stage" 0), or staged in shared memory one
+// plane ahead by per-thread 4-byte asynchronous copies (1) or by two tensor
+// copies per plane (TMA, box 32 x 8 x 1 x 15 of the f and g arrays) that
+// complete on an mbarrier (2).
 //
 // Eligible: FP32 storage, viscosity ratio 1 or the fixed-viscosity mode (the
 // step's tau_g then needs no phi range of the state it collides), band
 // forcing with kc <= 3 or no band forcing.
 #include "fast_common.cuh"
+
+#include <cuda.h>  // CUtensorMap and the encoder's enums (the encoder is resolved at run time)
 
 namespace dl {
 
@@ -57,22 +62,77 @@ __device__ __forceinline__ void cp_async4(float* smem_dst, const float* gmem_src
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// ---- tensor copies (TMA) completing on an mbarrier ----
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+    const unsigned b = (unsigned)__cvta_generic_to_shared(bar);
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(b), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
+    const unsigned b = (unsigned)__cvta_generic_to_shared(bar);
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(b), "r"(bytes) : "memory");
+}
+// box {32, 8, 1, 15} at (x, y, z, 0) of a 4-d map [15][nz][ny][nx] into dst
+__device__ __forceinline__ void tma_load_plane(float* dst, const CUtensorMap* map, unsigned long long* bar, int x,
+                                               int y, int z) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    const unsigned b = (unsigned)__cvta_generic_to_shared(bar);
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+        "[%6];\n" ::"r"(d),
+        "l"(reinterpret_cast<unsigned long long>(map)), "r"(x), "r"(y), "r"(z), "r"(0), "r"(b)
+        : "memory");
+}
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;\n" : "=l"(t));
+    return t;
+}
+// wait for the phase with the given parity to complete; false once limit_ns
+// nanoseconds have passed without it
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity, unsigned long long limit_ns) {
+    const unsigned b = (unsigned)__cvta_generic_to_shared(bar);
+    const unsigned long long t0 = global_ns();
+    for (;;) {
+        unsigned done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(b), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if (global_ns() - t0 > limit_ns) return false;
+    }
+}
+
 struct PushArgs {
     FastArgs a;
     int pending;           // the loaded populations lack the band force and wall reflection of their streaming
     int walls_load;        // reflect at the wall planes (pending and walls on)
     float wl_bot[5], wl_top[5];  // wall terms of the step whose streaming the load completes
+    unsigned long long wait_ns;  // stage 2: limit of a wait for the staged plane (option "wait_ns")
+    unsigned extra_tx;           // stage 2: bytes expected beyond the copies' (option "stage_extra_tx", tests
+                                 // of the limit: with it no phase completes and every block's wait runs out)
+    CUtensorMap tmf, tmg;  // stage 2: maps [15][nz][ny][nx] of the loaded f and g (box 32 x 8 x 1 x 15)
 };
 
 // staged populations of the next plane, one column per thread: [2 Q][NT]
 constexpr int PB_FLOATS = 2 * Q * NT;
 
 // shared-memory footprint in floats
-__host__ __device__ constexpr int push_smem_floats(bool spec, bool sp, bool bulk = false) {
-    return (bulk ? PB_FLOATS : 0) + (sp ? 0 : PSL * P1 * 4 + 2 * Q * NHALO) +
+// (rings and tables, then, stage 1 or 2, the staged plane at a 128-byte
+// offset, then, stage 2, its mbarrier and 128 bytes of room to move the plane
+// to a 128-byte boundary of the shared window, where tensor copies land)
+__host__ __device__ constexpr int push_rings_floats(bool spec, bool sp) {
+    return (sp ? 0 : PSL * P1 * 4 + 2 * Q * NHALO) +
            (spec ? PSL * P2 * FENT + 2 * (3 * SNK * EY2 * 2) + 3 * SNK * EY2 * 3 * 2 + SNK * EX2 * 2 +
                        SNK * EY2 * 2 + SNK * EX1 * 2 + SNK * EY1 * 2
                  : 0);
+}
+__host__ __device__ constexpr int push_stage_offset(bool spec, bool sp) { return (push_rings_floats(spec, sp) + 31) / 32 * 32; }
+__host__ __device__ constexpr int push_smem_floats(bool spec, bool sp, int stage = 0) {
+    return stage == 0 ? push_rings_floats(spec, sp) : push_stage_offset(spec, sp) + PB_FLOATS + (stage == 2 ? 36 : 0);
 }
 static_assert(PSL * P1 * 4 + PSL * P2 * FENT >= PT_SCRATCH, "projection scratch exceeds the rings");
 
@@ -378,11 +438,15 @@ __device__ __forceinline__ void push_minmax(const FastArgs& a, float bmin, float
 // the push-form kernel body. SP: the single-phase step (g only, no stencils).
 // SETTLE: no collision; complete the pending part of the loaded state in
 // place and write phi, u, p, the phi range and the band coefficients.
-// BULK: the thread's populations of the next plane arrive in shared memory by
-// asynchronous copies issued right after the barrier, one plane ahead, instead
-// of loads into registers issued after the collision
-template <bool LES, int FMODE, bool SP, bool SETTLE, bool BULK = false>
+// STG 1 and 2: the populations of the next plane arrive in shared memory,
+// copied one plane ahead right after the barrier, instead of loaded into
+// registers after the collision: by each thread for its own site (4-byte
+// asynchronous copies, STG 1), or by one thread for the block (two tensor
+// copies completing on an mbarrier, STG 2; full tiles only)
+template <bool LES, int FMODE, bool SP, bool SETTLE, int STG = 0>
 __device__ __forceinline__ void push_body(const PushArgs& pa, float* smem) {
+    constexpr bool BULK = STG != 0;
+    constexpr bool TMA = STG == 2;
     constexpr bool SPEC = FMODE == F_SPECTRAL;
     constexpr bool HALO = !SP && !SETTLE;  // the ring around the tile (stencils)
     constexpr bool NEEDG_HALO = LES;       // halo sites need u (strain) only with LES
@@ -396,7 +460,12 @@ __device__ __forceinline__ void push_body(const PushArgs& pa, float* smem) {
     float2* s_ty2 = s_tx2 + SNK * EX2;                             // [SNK][EY2] e^{i ky y}, y = y0-2+ey
     float2* s_tx1 = s_ty2 + SNK * EY2;                             // [SNK][EX1] projection tables
     float2* s_ty1 = s_tx1 + SNK * EX1;                             // [SNK][EY1]
-    float* s_pb = smem + push_smem_floats(SPEC, SP);                   // [2 Q][NT] staged plane (BULK)
+    float* s_pb = smem + push_stage_offset(SPEC, SP);                  // [2 Q][NT] staged plane (BULK)
+    if (TMA) {  // at a 128-byte boundary of the shared window (the room is in the footprint)
+        const unsigned off = (unsigned)__cvta_generic_to_shared(s_pb);
+        s_pb += ((128u - (off & 127u)) & 127u) / 4u;
+    }
+    unsigned long long* s_bar = reinterpret_cast<unsigned long long*>(s_pb + PB_FLOATS);  // (TMA)
 
     const int tid = threadIdx.x;
     const int tx = tid % TX, ty = tid / TX;
@@ -556,10 +625,25 @@ __device__ __forceinline__ void push_body(const PushArgs& pa, float* smem) {
     };
 
     // ---- staged planes (BULK) ----
-    // the thread's site of plane zp into its own column of s_pb (4-byte
-    // asynchronous copies, coalesced per warp; each thread reads back its own)
+    // STG 1: the thread's site of plane zp into its own column of s_pb (4-byte
+    // asynchronous copies, coalesced per warp; each thread reads back its own).
+    // STG 2: the tile of plane zp, 15 f then 15 g of 256 sites, in the same
+    // layout, by two tensor copies; every thread waits for the mbarrier's phase
+    // (the copies are issued after a barrier that follows every read of s_pb)
+    unsigned tph = 0;       // TMA: parity of the phase the next take waits for
+    bool tma_late = false;  // TMA: a wait of this thread ran out (the step reports DL_ERR_TIMEOUT);
+                            // thread 0 then issues no more copies and no more waits are made
     auto bulk_issue = [&](int zp) {
         if (!BULK) return;
+        if (TMA) {
+            if (tid == 0 && !tma_late) {
+                const int zw = wrap_near(zp, nz);
+                mbar_expect_tx(s_bar, (SP ? 1u : 2u) * Q * NT * (unsigned)sizeof(float) + pa.extra_tx);
+                if (!SP) tma_load_plane(s_pb, &pa.tmf, s_bar, x0, y0, zw);
+                tma_load_plane(s_pb + Q * NT, &pa.tmg, s_bar, x0, y0, zw);
+            }
+            return;
+        }
         const unsigned s = (unsigned)wrap_near(zp, nz) * nxy + col;
         if (!SP) {
 #pragma unroll
@@ -571,7 +655,15 @@ __device__ __forceinline__ void push_body(const PushArgs& pa, float* smem) {
     };
     auto bulk_take = [&](float* v) {
         if (!BULK) return;
-        cp_async_wait_all();
+        if (TMA) {
+            if (!tma_late && !mbar_wait(s_bar, tph, pa.wait_ns)) {
+                tma_late = true;
+                atomicExch(&a.st->wait_timeout, 1);
+            }
+            tph ^= 1u;
+        } else {
+            cp_async_wait_all();
+        }
         if (!SP) {
 #pragma unroll
             for (int i = 0; i < Q; ++i) v[i] = s_pb[i * NT + tid];
@@ -749,6 +841,10 @@ __device__ __forceinline__ void push_body(const PushArgs& pa, float* smem) {
         // ---- the march: collide plane t while plane t+1 arrives ----
         float A[2 * Q], B[2 * Q];
         float oA[5], oB[5];  // own moments (dphi, u1, u2, u3, dp) of the planes held in A, B
+        if (TMA) {
+            if (tid == 0) mbar_init(s_bar, 1);
+            __syncthreads();
+        }
         // planes zlo (= z0 - 1, moments only) and z0
         if (BULK) {
             bulk_issue(z0 - 1);
@@ -761,6 +857,7 @@ __device__ __forceinline__ void push_body(const PushArgs& pa, float* smem) {
         own_plane(z0 - 1, A, oA[0], oA[1], oA[2], oA[3], oA[4]);
         halo_plane(z0 - 1);
         if (BULK) {
+            if (TMA) __syncthreads();  // every thread has read plane z0-1 from s_pb
             bulk_issue(z0);
             issue_halo(z0);
             bulk_take(A);
@@ -780,6 +877,7 @@ __device__ __forceinline__ void push_body(const PushArgs& pa, float* smem) {
             __syncthreads();
         }
         if (BULK) {
+            if (TMA && !fpend) __syncthreads();  // every thread has read plane z0 from s_pb
             bulk_issue(z0 + 1);
         } else {
             issue(z0 + 1, col, B, !SP, true);
@@ -828,18 +926,24 @@ __device__ __forceinline__ void push_body(const PushArgs& pa, float* smem) {
     } else {
         push_minmax(a, bmin, bmax, bad, nblk);
     }
+    if (TMA && tid == 0 && tma_late) {
+        // copies issued before the wait ran out may still be in flight: keep the
+        // block, and with it its shared memory, a millisecond longer
+        const unsigned long long t0 = global_ns();
+        while (global_ns() - t0 < 1000000ull) __nanosleep(10000);
+    }
 }
 
-template <bool LES, int FMODE, bool BULK>
-__global__ void __launch_bounds__(NT, 2) step_push(const PushArgs pa) {
+template <bool LES, int FMODE, int STG>
+__global__ void __launch_bounds__(NT, 2) step_push(const __grid_constant__ PushArgs pa) {
     extern __shared__ __align__(128) float smem[];
-    push_body<LES, FMODE, false, false, BULK>(pa, smem);
+    push_body<LES, FMODE, false, false, STG>(pa, smem);
 }
 
-template <int FMODE, bool BULK>
-__global__ void __launch_bounds__(NT, 2) step_push_sp(const PushArgs pa) {
+template <int FMODE, int STG>
+__global__ void __launch_bounds__(NT, 2) step_push_sp(const __grid_constant__ PushArgs pa) {
     extern __shared__ __align__(128) float smem[];
-    push_body<false, FMODE, true, false, BULK>(pa, smem);
+    push_body<false, FMODE, true, false, STG>(pa, smem);
 }
 
 template <int FMODE, bool SP>
@@ -894,37 +998,77 @@ static dim3 push_grid(const dl_handle* h, int lz) {
     return dim3((h->nx + TX - 1) / TX, (h->ny + TY - 1) / TY, (h->nz + lz - 1) / lz);
 }
 
-// option "stage": the next plane's populations staged in shared memory
-static bool use_bulk(const dl_handle* h) { return h->push_bulk != 0; }
+// ---- option "stage" 2: tensor maps of the population buffers ----
+// f and g of each of the two buffers as 4-d FP32 tensors [15][nz][ny][nx]
+// (x innermost), box 32 x 8 x 1 x 15: one copy brings a tile's plane of all
+// 15 directions. The encoder is the driver's, resolved at run time (no link
+// against the driver library); the maps are made once per handle.
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
-template <bool LES, int FMODE, bool BULK>
+bool push_tma_eligible(const dl_handle* h) { return h->nx % TX == 0 && h->ny % TY == 0; }
+
+static int make_tmaps(dl_handle* h) {
+    if (h->push_tmap_ok) return DL_OK;
+    if (!push_tma_eligible(h)) return set_error(h, DL_ERR_UNSUPPORTED, "stage 2 needs nx %% %d == 0 and ny %% %d == 0", TX, TY);
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !fn)
+        return set_error(h, DL_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
+    const EncodeTiledFn encode = reinterpret_cast<EncodeTiledFn>(fn);
+    const cuuint64_t dims[4] = {(cuuint64_t)h->nx, (cuuint64_t)h->ny, (cuuint64_t)h->nz, (cuuint64_t)Q};
+    const cuuint64_t strides[3] = {(cuuint64_t)h->nx * 4, (cuuint64_t)h->nx * h->ny * 4, (cuuint64_t)h->N * 4};
+    const cuuint32_t box[4] = {TX, TY, 1, Q};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    void* bufs[4] = {h->fs[0], h->fs[1], h->gs[0], h->gs[1]};
+    static_assert(sizeof(CUtensorMap) == sizeof(h->push_tmap[0]), "tensor map size");
+    for (int k = 0; k < 4; ++k) {
+        if (!bufs[k]) continue;  // the single-phase step has no f
+        CUtensorMap m;
+        const CUresult r = encode(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, bufs[k], dims, strides, box, estr,
+                                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) return set_error(h, DL_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+        memcpy(h->push_tmap[k], &m, sizeof(m));
+    }
+    h->push_tmap_ok = 1;
+    return DL_OK;
+}
+
+template <bool LES, int FMODE, int STG>
 static int launch_push_t(dl_handle* h, const PushArgs& pa) {
     static bool done[64] = {false};
-    const size_t sm = sizeof(float) * (size_t)push_smem_floats(FMODE == F_SPECTRAL, false, BULK);
-    int rc = configure_smem(h, step_push<LES, FMODE, BULK>, sm, done);
+    const size_t sm = sizeof(float) * (size_t)push_smem_floats(FMODE == F_SPECTRAL, false, STG);
+    int rc = configure_smem(h, step_push<LES, FMODE, STG>, sm, done);
     if (rc != DL_OK) return rc;
-    DL_LAUNCH(h, true, (step_push<LES, FMODE, BULK><<<push_grid(h, pa.a.lz), NT, sm, h->stream>>>(pa)));
+    DL_LAUNCH(h, true, (step_push<LES, FMODE, STG><<<push_grid(h, pa.a.lz), NT, sm, h->stream>>>(pa)));
     DL_CUDA(h, cudaGetLastError());
     return DL_OK;
 }
 template <bool LES, int FMODE>
 static int launch_push(dl_handle* h, const PushArgs& pa) {
-    return use_bulk(h) ? launch_push_t<LES, FMODE, true>(h, pa) : launch_push_t<LES, FMODE, false>(h, pa);
+    return h->push_bulk == 2   ? launch_push_t<LES, FMODE, 2>(h, pa)
+           : h->push_bulk == 1 ? launch_push_t<LES, FMODE, 1>(h, pa)
+                               : launch_push_t<LES, FMODE, 0>(h, pa);
 }
 
-template <int FMODE, bool BULK>
+template <int FMODE, int STG>
 static int launch_push_sp_t(dl_handle* h, const PushArgs& pa) {
     static bool done[64] = {false};
-    const size_t sm = sizeof(float) * (size_t)push_smem_floats(FMODE == F_SPECTRAL, true, BULK);
-    int rc = configure_smem(h, step_push_sp<FMODE, BULK>, sm, done);
+    const size_t sm = sizeof(float) * (size_t)push_smem_floats(FMODE == F_SPECTRAL, true, STG);
+    int rc = configure_smem(h, step_push_sp<FMODE, STG>, sm, done);
     if (rc != DL_OK) return rc;
-    DL_LAUNCH(h, true, (step_push_sp<FMODE, BULK><<<push_grid(h, pa.a.lz), NT, sm, h->stream>>>(pa)));
+    DL_LAUNCH(h, true, (step_push_sp<FMODE, STG><<<push_grid(h, pa.a.lz), NT, sm, h->stream>>>(pa)));
     DL_CUDA(h, cudaGetLastError());
     return DL_OK;
 }
 template <int FMODE>
 static int launch_push_sp(dl_handle* h, const PushArgs& pa) {
-    return use_bulk(h) ? launch_push_sp_t<FMODE, true>(h, pa) : launch_push_sp_t<FMODE, false>(h, pa);
+    return h->push_bulk == 2   ? launch_push_sp_t<FMODE, 2>(h, pa)
+           : h->push_bulk == 1 ? launch_push_sp_t<FMODE, 1>(h, pa)
+                               : launch_push_sp_t<FMODE, 0>(h, pa);
 }
 
 template <int FMODE, bool SP>
@@ -941,6 +1085,14 @@ static int launch_settle(dl_handle* h, const PushArgs& pa) {
 int push_step(dl_handle* h) {
     PushArgs pa;
     push_args(h, pa, false);
+    if (h->push_bulk == 2) {
+        const int rc = make_tmaps(h);
+        if (rc != DL_OK) return rc;
+        pa.wait_ns = (unsigned long long)h->push_wait_ns;
+        pa.extra_tx = (unsigned)h->push_extra_tx;
+        memcpy(&pa.tmf, h->push_tmap[h->cur], sizeof(pa.tmf));
+        memcpy(&pa.tmg, h->push_tmap[2 + h->cur], sizeof(pa.tmg));
+    }
     const int fmode = force_fmode(h);
     int rc;
     if (h->single) {

@@ -299,8 +299,19 @@ int dl_profile_read(dl_handle* h, dl_profile_stats* out);
  * phase): the next plane's pulls held in registers. "projection" 0|1 (band
  * forcing, default 1): the projection of the new u on the band modes done by
  * each block of the fused step after its march, else by a launch of its own;
- * both give the same coefficients up to the FP32 summation order. Read back
- * with dl_get_option. Returns DL_ERR_ARG for an unknown key or value. */
+ * both give the same coefficients up to the FP32 summation order. "push" 0|1
+ * (FP32, default 1): step in the push form where eligible (read-only keys
+ * "push_eligible" and "pushed" report it). "stage" (push form) 0: the next
+ * plane's populations loaded into registers (two-phase default); 1: staged in
+ * shared memory by per-thread asynchronous copies (single-phase default); 2:
+ * staged by two tensor (TMA) copies per plane completing on an mbarrier
+ * (nx a multiple of 32 and ny of 8, else DL_ERR_UNSUPPORTED); all three give
+ * the same bits. "wait_ns" (stage 2, default 2e9): the time limit of a
+ * block's wait for its staged plane; when it runs out the block stops
+ * waiting and dl_sync returns DL_ERR_TIMEOUT. "stage_extra_tx" (stage 2,
+ * default 0; for tests of that limit): bytes the mbarrier expects beyond the
+ * copies', so that no wait completes. Read back with dl_get_option. Returns
+ * DL_ERR_ARG for an unknown key or value. */
 int dl_set_option(dl_handle* h, const char* key, int64_t value);
 int dl_get_option(dl_handle* h, const char* key, int64_t* value);
 

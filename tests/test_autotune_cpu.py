@@ -75,7 +75,13 @@ def test_tuner_push_form_tunes_staging(tmp_path, monkeypatch):
     monkeypatch.setattr(autotune, "gpu_name", lambda: "fake-gpu")
     sim = FakePushSim()
     r = autotune.tune_droplet(sim, steps=5)
-    assert r["lz"] == 16 and r["stage"] == 1 and "prefetch" not in r and sim.stage == 1
+    # full 32 x 8 tiles: the tensor-copy staging (2) is a candidate
+    assert r["lz"] == 16 and r["stage"] == 2 and "prefetch" not in r and sim.stage == 2
+    # a partial tile in x: stages 0 and 1 only
+    sim2 = FakePushSim()
+    sim2.nx = 40
+    r2 = autotune.tune_droplet(sim2, steps=5)
+    assert r2["stage"] == 1 and sim2.stage == 1 and not r2["cached"]
 
 
 class FakeEnsemble:

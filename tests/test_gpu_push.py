@@ -14,6 +14,7 @@ import pytest
 
 from droplet_gb300 import configs
 from droplet_gb300 import _abi
+from droplet_gb300._lib import DropletError
 from droplet_gb300.solver import Droplet, FORM_FP32
 from oracle import pyoracle
 
@@ -159,3 +160,77 @@ def test_push_bitwise_independent_of_z_chunks():
         out.append(g.get_fields())
     for k in out[0]:
         assert np.array_equal(out[0][k], out[1][k]) and np.array_equal(out[0][k], out[2][k]), k
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_tensor_staged_planes_equal_loaded_planes(case):
+    """The next plane staged by two tensor (TMA) copies per block and plane,
+    completing on an mbarrier (option "stage" = 2; full tiles), gives the same
+    bits as the per-thread copies and as loads into registers."""
+    shape = (64, 16, 14)
+    P, f, mode, force = make_case(case, shape)
+    out = {}
+    for stage in (0, 1, 2):
+        g = Droplet(P, shape, FORM_FP32)
+        g.set_option("stage", stage)
+        start(g, f, mode, force)
+        g.step(9)
+        out[stage] = (g.get_fields(), g.get_populations())
+        g.sync()
+    for stage in (1, 2):
+        for k in out[0][0]:
+            assert np.array_equal(out[0][0][k], out[stage][0][k]), (stage, k)
+        for j in (0, 1):
+            assert np.array_equal(out[0][1][j], out[stage][1][j]), (stage, j)
+
+
+def test_tensor_staged_single_phase():
+    """The precursor step (g only, band forcing) with its plane staged by one
+    tensor copy per block and plane: the same bits as the per-thread copies."""
+    w = configs.precursor(n=32)
+    out = {}
+    for stage in (1, 2):
+        g = Droplet(w.params, (32, 32, 32), FORM_FP32, single_phase=True)
+        g.set_option("stage", stage)
+        g.set_fields(**w.fields)
+        g.init_equilibrium()
+        g.set_force(_abi.DL_FORCE_SPECTRAL)
+        g.step(12)
+        out[stage] = g.get_fields()
+        g.sync()
+    for k in out[1]:
+        assert np.array_equal(out[1][k], out[2][k]), k
+
+
+def test_tensor_stage_needs_full_tiles():
+    P, f, mode, force = make_case("plain", (40, 16, 8))
+    g = Droplet(P, (40, 16, 8), FORM_FP32)
+    with pytest.raises(DropletError) as e:
+        g.set_option("stage", 2)
+    assert e.value.status == _abi.DL_ERR_UNSUPPORTED
+    assert g.get_option("stage") == 0
+
+
+def test_tensor_stage_wait_limit_reports_timeout():
+    """The blocks' waits for the staged plane are bounded in time: with the
+    mbarrier told to expect 16 bytes more than the copies bring, no phase
+    completes, every block gives up after "wait_ns", the step finishes and
+    dl_sync reports DL_ERR_TIMEOUT; the device stays usable."""
+    shape = (64, 16, 12)
+    P, f, mode, force = make_case("plain", shape)
+    g = Droplet(P, shape, FORM_FP32)
+    g.set_option("stage", 2)
+    g.set_option("wait_ns", 200000)
+    g.set_option("stage_extra_tx", 16)
+    start(g, f, mode, force)
+    g.step(2)
+    with pytest.raises(DropletError) as e:
+        g.sync()
+    assert e.value.status == _abi.DL_ERR_TIMEOUT
+    g.close()
+    h = Droplet(P, shape, FORM_FP32)
+    h.set_option("stage", 2)
+    start(h, f, mode, force)
+    h.step(3)
+    h.sync()
+    assert np.isfinite(h.get_fields()["phi"]).all()
