@@ -13,16 +13,23 @@
 //   A = p0(phi) - kf phi lap(phi) - kf/6 |grad phi|^2,
 //   cGc_i = 4.5 (c_i.grad phi)^2 - 1.5 |c_i|^2 |grad phi|^2,
 //   phi = sum f, p = sum g / 3, u = sum c g.
+// With the Smagorinsky term (program/LES_drop_xy.f90:481-502, 663-690) wg is
+// per site: tau_g = 1/2 + 3 (nu + nu_t)/ds, nu_t = csd sqrt(2 S:S), S the
+// symmetric part of G_ab = d u_a / d x_b from the 14-neighbour stencil of u;
+// its adjoint needs the pre-step g (the adjoint state then carries it) and
+// sends dL/dG back to u through the transposed stencil.
 // Reverse of one step = three launches:
 //   adj_walls   reflected adjoints at the wall planes, d/dU;
 //   adj_local   per source site y: gather a_i = lf'_i(y + c_i), b_i = lg'_i(y + c_i)
 //               and form the local adjoints of phi, A (-> lap, |grad|^2), grad phi,
 //               u, p; d/dkf, d/dkg, d/dwf;
-//   adj_stencil per site x: transpose of the lap/grad stencils, then
-//               lf_i = (1-wf) a_i + lphi, lg_i = (1-wg) b_i + lp/3 + c_i.lu.
+//   adj_stencil per site x: transpose of the lap/grad stencils (and, LES, of
+//               the u stencil), then
+//               lf_i = (1-wf) a_i + lphi, lg_i = (1-wg(x)) b_i + lp/3 + c_i.lu.
 // States are in the FP32 form's layout: df[15][N] (deviations from the bulk
-// equilibrium) followed by dphi, u1, u2, u3, dp [5][N] (the adjoint state), or
-// df, dg[15][N], fields (the full state of the initial step).
+// equilibrium) followed by dphi, u1, u2, u3, dp [5][N] and, with LES, dg[15][N]
+// (the adjoint state), or df, dg[15][N], fields (the full state of the initial
+// step).
 #include "dl_internal.cuh"
 #include "dl_device.cuh"
 
@@ -36,16 +43,21 @@ struct AdjArgs {
     unsigned N;
     const float* st;      // forward f before the step: df[15N]
     const float* mac;     // forward fields before the step: [5][N]
+    const float* gst;     // LES: forward g before the step: dg[15N]
     const float* lin;     // adjoint of the post-step populations, [30][N] (f then g)
     float* lout;          // adjoint of the pre-step populations, [30][N]
-    float* aux;           // [9][N]: lphi_loc, llap, lgrad x y z, lp, lu x y z
+    float* aux;           // [9][N]: lphi_loc, llap, lgrad x y z, lp, lu x y z; LES: + [9][N] dL/dG_ab
+                          // (a + 3 b) and [1][N] wg
     double* grads;        // [ADJ_NREP][4]: d/dkf, d/dkg, d/dwf, d/dU (block b adds to copy b % ADJ_NREP)
     float phi1, omf, omg, kf, kf6, kg, T, a, b, inv_lap, inv_grad;
     float fref[Q];
     float wbot[5], wtop[5];   // d g'_i / dU at the bottom / top wall, per reflected pair
     int walls_on;             // the walls moved in this step
     int stream;               // 1: a time step; 0: the initial f = feq, g = geq
+    int les;                  // Smagorinsky eddy viscosity in tau_g (time steps)
+    float csd, nu1, inv_ds;   // LES: (Cs delta)^2, nu, 1/ds
 };
+constexpr int ADJ_AUX = 19;  // aux rows allocated (9, and 10 more with LES)
 
 constexpr int ADJ_NREP = 64;  // copies of the gradient accumulators (spreads the atomics)
 
@@ -138,11 +150,48 @@ __global__ void __launch_bounds__(256) adj_local(AdjArgs a) {
     const float p0ref = a.phi1 * a.T / (1.f - a.b * a.phi1) - a.a * a.phi1 * a.phi1;
     const float dp0 = a.T / (omb * omb) - 2.f * a.a * phi;
     const float dA = (p0 - p0ref) - a.kf * phi * lap - a.kf6 * gsq;
+    // LES: G_ab = d u_a / d x_b, S, nu_t, wg of this site
+    const bool les = a.les && a.stream;
+    float G[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+    float tt = 0.f, wgs = a.omg;
+    if (les) {
+#pragma unroll
+        for (int k = 1; k < Q; ++k) {
+            const unsigned m = nbr(a, x, y, z, cx(k), cy(k), cz(k));
+            const float uk[3] = {mac[N + m], mac[2 * N + m], mac[3 * N + m]};
+#pragma unroll
+            for (int al = 0; al < 3; ++al) {
+                if (cx(k)) G[al][0] += cx(k) * uk[al];
+                if (cy(k)) G[al][1] += cy(k) * uk[al];
+                if (cz(k)) G[al][2] += cz(k) * uk[al];
+            }
+        }
+        float acc = 0.f;
+#pragma unroll
+        for (int al = 0; al < 3; ++al)
+#pragma unroll
+            for (int be = 0; be < 3; ++be) {
+                G[al][be] *= a.inv_grad;
+            }
+#pragma unroll
+        for (int al = 0; al < 3; ++al)
+#pragma unroll
+            for (int be = 0; be < 3; ++be) {
+                const float sab = 0.5f * (G[al][be] + G[be][al]);
+                acc += sab * sab;
+            }
+        tt = 2.f * acc;
+        const float nut = tt > 0.f ? a.csd * sqrtf(tt) : 0.f;
+        wgs = 1.f / (0.5f + 3.f * (a.nu1 + nut) * a.inv_ds);
+    }
+    float lw = 0.f;  // LES: dL/dwg of this site
     float lphi = 0.f, lA = 0.f, lp = 0.f, lusq = 0.f, lgsq = 0.f;
     float lu[3] = {0.f, 0.f, 0.f}, lgr[3] = {0.f, 0.f, 0.f};
     // per-site sums in FP32 (15 terms); FP64 from the block sums on (GB300's FP64 rate is low)
     float dkf = 0.f, dkg = 0.f, domf = 0.f;
-    const float wf = a.stream ? a.omf : 1.f, wg = a.stream ? a.omg : 1.f;
+    const float wf = a.stream ? a.omf : 1.f, wg = a.stream ? wgs : 1.f;
+    const float dp = mac[4 * N + s];
+    const float usq = u1 * u1 + u2 * u2 + u3 * u3;
 #pragma unroll
     for (int i = 0; i < Q; ++i) {
         const unsigned src = a.stream ? nbr(a, x, y, z, cx(i), cy(i), cz(i)) : s;
@@ -156,6 +205,10 @@ __global__ void __launch_bounds__(256) adj_local(AdjArgs a) {
         if (a.stream) {
             const float dfeq = HW(i) * dphi + FW(i) * dA + E * (3.f * phi * cu + a.kf * cGc);
             domf += ai * (dfeq - a.st[(size_t)i * N + s]);
+        }
+        if (les) {  // geq_i - g_i in deviations (the bulk E_i cancels)
+            const float dgeq = E * (3.f * dp + 3.f * cu + 4.5f * cu * cu - 1.5f * usq + a.kg * cGc);
+            lw += bi * (dgeq - a.gst[(size_t)i * N + s]);
         }
         lphi += Lf * (HW(i) + 3.f * E * cu);
         lA += Lf * FW(i);
@@ -194,6 +247,16 @@ __global__ void __launch_bounds__(256) adj_local(AdjArgs a) {
         a.aux[6 * N + s] = lu[0];
         a.aux[7 * N + s] = lu[1];
         a.aux[8 * N + s] = lu[2];
+        if (a.les) {
+            // dwg/dnu_t = -3 wg^2 / ds, dnu_t/dtt = csd / (2 sqrt(tt)), dtt/dG_ab = 4 S_ab
+            const float ltt = (les && tt > 0.f) ? lw * (-3.f * wgs * wgs * a.inv_ds) * (0.5f * a.csd / sqrtf(tt)) : 0.f;
+#pragma unroll
+            for (int al = 0; al < 3; ++al)
+#pragma unroll
+                for (int be = 0; be < 3; ++be)
+                    a.aux[(size_t)(9 + al + 3 * be) * N + s] = ltt * 2.f * (G[al][be] + G[be][al]);
+            a.aux[(size_t)18 * N + s] = wg;
+        }
     } else {
         dkf = dkg = domf = 0.f;
     }
@@ -217,11 +280,33 @@ __global__ void __launch_bounds__(256) adj_stencil(AdjArgs a, float* phi_out) {
                 a.inv_grad * (cx(k) * a.aux[2 * N + m] + cy(k) * a.aux[3 * N + m] + cz(k) * a.aux[4 * N + m]);
     }
     const float lp = a.aux[5 * N + s] * (1.f / 3.f);
-    const float lu1 = a.aux[6 * N + s], lu2 = a.aux[7 * N + s], lu3 = a.aux[8 * N + s];
+    float lu1 = a.aux[6 * N + s], lu2 = a.aux[7 * N + s], lu3 = a.aux[8 * N + s];
+    float wg = a.stream ? a.omg : 1.f;
+    if (a.les && a.stream) {
+        // transpose of G_ab(y) = inv_grad sum_k c_kb u_a(y + c_k): u_a(x) receives
+        // inv_grad c_kb dL/dG_ab(x - c_k)
+        float t[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+        for (int k = 1; k < Q; ++k) {
+            const unsigned m = nbr(a, x, y, z, -cx(k), -cy(k), -cz(k));
+#pragma unroll
+            for (int al = 0; al < 3; ++al) {
+                float v = 0.f;
+                if (cx(k)) v += cx(k) * a.aux[(size_t)(9 + al) * N + m];
+                if (cy(k)) v += cy(k) * a.aux[(size_t)(9 + al + 3) * N + m];
+                if (cz(k)) v += cz(k) * a.aux[(size_t)(9 + al + 6) * N + m];
+                t[al] += v;
+            }
+        }
+        lu1 += a.inv_grad * t[0];
+        lu2 += a.inv_grad * t[1];
+        lu3 += a.inv_grad * t[2];
+        wg = a.aux[(size_t)18 * N + s];
+    }
     if (phi_out) phi_out[s] = lphi;
     // the streamed part (1 - w) of the collision, gathered here rather than
     // stored by adj_local and read back
-    const float wf = a.stream ? a.omf : 1.f, wg = a.stream ? a.omg : 1.f;
+    const float wf = a.stream ? a.omf : 1.f;
 #pragma unroll
     for (int i = 0; i < Q; ++i) {
         const unsigned src = a.stream ? nbr(a, x, y, z, cx(i), cy(i), cz(i)) : s;
@@ -267,19 +352,23 @@ static void fill_adj(dl_handle* h, AdjArgs& a) {
     }
     a.grads = h->adj_grads;
     a.aux = h->adj_aux;
+    a.les = P.les ? 1 : 0;
+    a.csd = (float)(P.Cs * P.Cs * P.delta * P.delta);
+    a.nu1 = (float)P.nu1;
+    a.inv_ds = (float)(1.0 / P.ds);
 }
 
 int adjoint_check(dl_handle* h) {
     if (h->form != DL_FORM_FP32 || h->single)
         return set_error(h, DL_ERR_UNSUPPORTED, "the adjoint is implemented for the two-phase FP32 form");
-    if (h->P.les) return set_error(h, DL_ERR_UNSUPPORTED, "the adjoint does not cover the Smagorinsky term");
+    if (h->P.les && h->P.Anu != 0.0) return set_error(h, DL_ERR_UNSUPPORTED, "the adjoint assumes A_nu = 0");
     if (h->P.nu2 != h->P.nu1) return set_error(h, DL_ERR_UNSUPPORTED, "the adjoint assumes viscosity ratio 1");
     if (h->force_mode == DL_FORCE_SPECTRAL) return set_error(h, DL_ERR_UNSUPPORTED, "the adjoint covers no spectral force");
     if (h->P.wall_u[1] != 0.0 || h->P.wall_u[2] != 0.0)
         return set_error(h, DL_ERR_UNSUPPORTED, "the adjoint assumes an x wall velocity");
     if (!h->adj_lam[0]) {
         for (int k = 0; k < 2; ++k) DL_CUDA(h, cudaMalloc(&h->adj_lam[k], sizeof(float) * 30 * h->N));
-        DL_CUDA(h, cudaMalloc(&h->adj_aux, sizeof(float) * 9 * h->N));
+        DL_CUDA(h, cudaMalloc(&h->adj_aux, sizeof(float) * ADJ_AUX * h->N));
         DL_CUDA(h, cudaMalloc(&h->adj_grads, sizeof(double) * 4 * ADJ_NREP));
     }
     return DL_OK;
@@ -313,8 +402,9 @@ int adjoint_step(dl_handle* h, const float* d_state, long long step) {
     if (rc != DL_OK) return rc;
     AdjArgs a;
     fill_adj(h, a);
-    a.st = d_state;                           // adjoint state: f[15N], fields[5N]
+    a.st = d_state;                           // adjoint state: f[15N], fields[5N] (, g[15N])
     a.mac = d_state + (size_t)Q * h->N;
+    a.gst = d_state + (size_t)20 * h->N;
     a.lin = h->adj_lam[h->adj_cur];
     a.lout = h->adj_lam[1 - h->adj_cur];
     a.stream = 1;

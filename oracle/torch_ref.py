@@ -2,7 +2,9 @@
 
 Used as the "plain PyTorch autodiff reference" for the hand-written adjoint:
 the same physics as the C oracle (program/lbm_drop_xy.f90:421-666 with the
-moving-wall bounce-back of prototype_program/two-phase/drop8_mpi.f90:642-674),
+moving-wall bounce-back of prototype_program/two-phase/drop8_mpi.f90:642-674
+and, when P.les, the Smagorinsky tau_g of program/LES_drop_xy.f90:481-502,
+663-690),
 written with torch.roll so that autograd differentiates it, in FP64. It does
 not follow the reference's evaluation order (it is not a parity restatement);
 its job is gradients.
@@ -64,11 +66,34 @@ def moments(f, g):
     return phi, u, p
 
 
+def les_taug(P, u):
+    """tau_g = 1/2 + 3 (nu1 + nu_t)/ds, nu_t = (Cs delta)^2 sqrt(2 S:S), S the
+    symmetric part of d u_a / d x_b from the 14-neighbour stencil."""
+    G = [[None] * 3 for _ in range(3)]
+    for a in range(3):
+        for b in range(3):
+            s = torch.zeros_like(u[a])
+            for i in range(1, 15):
+                c = (CX, CY, CZ)[b][i]
+                if c:
+                    s = s + c * nb(u[a], i)
+            G[a][b] = s / (10.0 * P.ds)
+    acc = torch.zeros_like(u[0])
+    for a in range(3):
+        for b in range(3):
+            acc = acc + (0.5 * (G[a][b] + G[b][a])) ** 2
+    nut = (P.Cs * P.delta) ** 2 * torch.sqrt((2.0 * acc).clamp_min(1e-300))
+    return 0.5 + 3.0 * (P.nu1 + nut) / P.ds
+
+
 def step(P, f, g, kf, kg, tauf, U, taug):
-    """One time step with constant tau_g (viscosity ratio 1). U: top-wall
-    x velocity (tensor); the bottom wall moves with -U."""
+    """One time step at viscosity ratio 1: tau_g constant, or from the
+    Smagorinsky strain when P.les. U: top-wall x velocity (tensor); the
+    bottom wall moves with -U."""
     phi, u, p = moments(f, g)
     feq, geq = equilibria(P, phi, u, p, kf, kg)
+    if P.les:
+        taug = les_taug(P, u)
     fn = [nb(f[i] - (f[i] - feq[i]) / tauf, i, -1) for i in range(15)]
     gn = [nb(g[i] - (g[i] - geq[i]) / taug, i, -1) for i in range(15)]
     if P.walls:

@@ -1,8 +1,11 @@
 """The hand-written adjoint of the FP32 step (through the C-ABI) against
 (1) a plain PyTorch autodiff restatement in FP64 and (2) central finite
 differences (relative step 1e-4) of the FP64 plain form, on the shear-droplet
-physics at 32^3 over 100 steps. Tolerances: 2 % relative for the scalar
-gradients, 5 % relative L2 for dD/dphi0 (FP32 adjoint vs FP64 references)."""
+physics at 32^3 over 100 steps, and with the Smagorinsky eddy viscosity over
+60 steps (Cs = 2, large enough that nu_t is about a tenth of nu and leaving
+its adjoint out moves the gradients by more than the tolerance). Tolerances:
+2 % relative for the scalar gradients, 5 % relative L2 for dD/dphi0 (FP32
+adjoint vs FP64 references)."""
 import numpy as np
 import pytest
 import torch
@@ -22,11 +25,11 @@ def case():
     return w
 
 
-def fp64_loss(P, w):
+def fp64_loss(P, w, nsteps=NSTEPS):
     g = Droplet(P, w.shape, FORM_FP64)
     g.set_fields(**w.fields)
     g.init_equilibrium()
-    g.step(NSTEPS)
+    g.step(nsteps)
     D, _ = deformation_and_grad(g.get_fields()["phi"], P.phi1, P.phi2)
     g.close()
     return D
@@ -108,3 +111,60 @@ def test_recomputed_segments_give_the_stored_run_gradients(adjoint_result):
     for name in ("dkappaf", "dkappag", "dtauf", "dU"):
         assert abs(g2[name] - g[name]) <= 1e-9 * abs(g[name]) + 1e-15, name
     assert np.array_equal(g2["dphi0"], g["dphi0"])
+
+
+LES_STEPS = 60
+
+
+def case_les():
+    w = configs.shear_droplet(n=32, radius=6.0, U=0.04, steps=LES_STEPS, form=32)
+    w.params = w.params.replace(les=1, Cs=2.0, delta=1.0)
+    return w
+
+
+def torch_grads(P, f, nsteps, les):
+    T = lambda a: torch.tensor(a, dtype=torch.float64)  # noqa: E731
+    phi0 = T(f["phi"]).requires_grad_(True)
+    ps = [torch.tensor(v, dtype=torch.float64, requires_grad=True)
+          for v in (P.kappaf, P.kappag, P.tauf, P.wall_u[0])]
+    taug = 0.5 + 3.0 * P.nu1 / P.ds
+    L = torch_ref.run_loss(P.replace(les=1 if les else 0), phi0, [T(f["u1"]), T(f["u2"]), T(f["u3"])], T(f["p"]),
+                           *ps, taug, nsteps)
+    L.backward()
+    out = {k: p.grad.item() for k, p in zip(("dkappaf", "dkappag", "dtauf", "dU"), ps)}
+    out["dphi0"] = phi0.grad.numpy()
+    out["D"] = L.item()
+    return out
+
+
+@pytest.fixture(scope="module")
+def adjoint_les():
+    w = case_les()
+    f = w.fields
+    run = CheckpointedRun(w.params, w.shape, (f["u1"], f["u2"], f["u3"]), f["p"], LES_STEPS)
+    D = run.forward(f["phi"])
+    g = run.backward()
+    run.close()
+    return w, D, g, torch_grads(w.params, f, LES_STEPS, True)
+
+
+def test_adjoint_les_matches_torch_autodiff(adjoint_les):
+    w, D, g, ref = adjoint_les
+    assert abs(ref["D"] - D) <= 1e-4 * abs(ref["D"])
+    for name in ("dkappaf", "dkappag", "dtauf", "dU"):
+        assert abs(g[name] - ref[name]) <= 2e-2 * abs(ref[name]) + 1e-12, (name, g[name], ref[name])
+    rel = np.linalg.norm(g["dphi0"] - ref["dphi0"]) / np.linalg.norm(ref["dphi0"])
+    assert rel <= 5e-2, rel
+    # the test has teeth: without the eddy viscosity the reference gradients differ by more
+    plain = torch_grads(w.params, w.fields, LES_STEPS, False)
+    assert max(abs(plain[k] - ref[k]) / abs(ref[k]) for k in ("dtauf", "dU", "dkappag")) > 5e-2
+
+
+def test_adjoint_les_matches_fp64_finite_differences(adjoint_les):
+    w, D, g, _ = adjoint_les
+    P = w.params
+    for name, mk, base in (("dkappag", lambda h: P.replace(kappag=P.kappag + h), P.kappag),
+                           ("dU", lambda h: P.replace(wall_u=(P.wall_u[0] + h, 0.0, 0.0)), P.wall_u[0])):
+        h = 1e-4 * abs(base)
+        fd = (fp64_loss(mk(h), w, LES_STEPS) - fp64_loss(mk(-h), w, LES_STEPS)) / (2 * h)
+        assert abs(g[name] - fd) <= 2e-2 * abs(fd) + 1e-12, (name, g[name], fd)
