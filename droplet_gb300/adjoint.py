@@ -89,7 +89,7 @@ class CheckpointedRun:
     coordinates and the eigen data."""
 
     def __init__(self, params: Params, shape, u0, p0, nsteps: int, segment: int | None = None,
-                 memory_fraction: float = 0.6):
+                 memory_fraction: float = 0.6, force_mode: int = 0):
         import torch
 
         self.torch = torch
@@ -98,6 +98,7 @@ class CheckpointedRun:
         self.u0 = [np.ascontiguousarray(u, dtype=np.float64) for u in u0]
         self.p0 = np.ascontiguousarray(p0, dtype=np.float64)
         self.nsteps = int(nsteps)
+        self.force_mode = int(force_mode)  # DL_FORCE_NONE or DL_FORCE_SPECTRAL (band forcing from u)
         self.timing = AdjointTiming()
         self.sim = None
         self._seg = None
@@ -135,6 +136,8 @@ class CheckpointedRun:
         self.sim.step_count = 0
         self.sim.set_fields(phi0, self.u0[0], self.u0[1], self.u0[2], self.p0)
         self.sim.init_equilibrium()
+        if self.force_mode:
+            self.sim.set_force(self.force_mode)
         for k in range(self.nsteps):
             if k % self.S == 0:
                 self.sim._call("save_state", C.c_void_p(self.ckpt[k // self.S].data_ptr()))
@@ -221,7 +224,8 @@ def _function():
         def forward(ctx, phi0, kappaf, kappag, tauf, wall_u, spec):
             P = spec["params"].replace(kappaf=float(kappaf), kappag=float(kappag), tauf=float(tauf),
                                        wall_u=(float(wall_u), 0.0, 0.0))
-            run = CheckpointedRun(P, spec["shape"], spec["u0"], spec["p0"], spec["nsteps"], spec.get("segment"))
+            run = CheckpointedRun(P, spec["shape"], spec["u0"], spec["p0"], spec["nsteps"], spec.get("segment"),
+                                  force_mode=spec.get("force_mode", 0))
             D = run.forward(phi0.detach().double().cpu().numpy())
             ctx.run = run
             ctx.device = phi0.device
@@ -242,5 +246,5 @@ def _function():
 def deformation_loss(phi0, kappaf, kappag, tauf, wall_u, spec):
     """torch entry point: returns D as a 0-dim tensor; gradients flow to phi0,
     kappaf, kappag, tauf and wall_u. spec: params (Params template), shape
-    (nx, ny, nz), u0 (three arrays), p0, nsteps[, segment]."""
+    (nx, ny, nz), u0 (three arrays), p0, nsteps[, segment][, force_mode]."""
     return _function().apply(phi0, kappaf, kappag, tauf, wall_u, spec)

@@ -17,7 +17,11 @@
 // per site: tau_g = 1/2 + 3 (nu + nu_t)/ds, nu_t = csd sqrt(2 S:S), S the
 // symmetric part of G_ab = d u_a / d x_b from the 14-neighbour stencil of u;
 // its adjoint needs the pre-step g (the adjoint state then carries it) and
-// sends dL/dG back to u through the transposed stencil.
+// sends dL/dG back to u through the transposed stencil. With the band force
+// (program/lbm_drop_iht_xy.f90:722-842), g'_i(x) gains 3 E_i c_i . F(x - c_i),
+// F = (0.5 eps / E(u)) P u from the band projection P of the pre-step u:
+// adj_local forms dL/dF(y) = sum_i 3 E_i c_i b_i(y) and spectral_adjoint_f32
+// adds its pull-back onto u (through P and through E) to lu.
 // Reverse of one step = three launches:
 //   adj_walls   reflected adjoints at the wall planes, d/dU;
 //   adj_local   per source site y: gather a_i = lf'_i(y + c_i), b_i = lg'_i(y + c_i)
@@ -55,9 +59,10 @@ struct AdjArgs {
     int walls_on;             // the walls moved in this step
     int stream;               // 1: a time step; 0: the initial f = feq, g = geq
     int les;                  // Smagorinsky eddy viscosity in tau_g (time steps)
+    int spec;                 // band force (time steps): aux rows 19..21 receive dL/dF
     float csd, nu1, inv_ds;   // LES: (Cs delta)^2, nu, 1/ds
 };
-constexpr int ADJ_AUX = 19;  // aux rows allocated (9, and 10 more with LES)
+constexpr int ADJ_AUX = 22;  // aux rows: 9, LES 10 more (9 .. 18), band force 3 more (19 .. 21)
 
 constexpr int ADJ_NREP = 64;  // copies of the gradient accumulators (spreads the atomics)
 
@@ -185,6 +190,7 @@ __global__ void __launch_bounds__(256) adj_local(AdjArgs a) {
         wgs = 1.f / (0.5f + 3.f * (a.nu1 + nut) * a.inv_ds);
     }
     float lw = 0.f;  // LES: dL/dwg of this site
+    float lF[3] = {0.f, 0.f, 0.f};  // band force: dL/dF of this site
     float lphi = 0.f, lA = 0.f, lp = 0.f, lusq = 0.f, lgsq = 0.f;
     float lu[3] = {0.f, 0.f, 0.f}, lgr[3] = {0.f, 0.f, 0.f};
     // per-site sums in FP32 (15 terms); FP64 from the block sums on (GB300's FP64 rate is low)
@@ -205,6 +211,11 @@ __global__ void __launch_bounds__(256) adj_local(AdjArgs a) {
         if (a.stream) {
             const float dfeq = HW(i) * dphi + FW(i) * dA + E * (3.f * phi * cu + a.kf * cGc);
             domf += ai * (dfeq - a.st[(size_t)i * N + s]);
+        }
+        if (a.spec && a.stream) {
+            lF[0] += 3.f * E * cx(i) * bi;
+            lF[1] += 3.f * E * cy(i) * bi;
+            lF[2] += 3.f * E * cz(i) * bi;
         }
         if (les) {  // geq_i - g_i in deviations (the bulk E_i cancels)
             const float dgeq = E * (3.f * dp + 3.f * cu + 4.5f * cu * cu - 1.5f * usq + a.kg * cGc);
@@ -256,6 +267,11 @@ __global__ void __launch_bounds__(256) adj_local(AdjArgs a) {
                 for (int be = 0; be < 3; ++be)
                     a.aux[(size_t)(9 + al + 3 * be) * N + s] = ltt * 2.f * (G[al][be] + G[be][al]);
             a.aux[(size_t)18 * N + s] = wg;
+        }
+        if (a.spec) {
+            a.aux[(size_t)19 * N + s] = lF[0];
+            a.aux[(size_t)20 * N + s] = lF[1];
+            a.aux[(size_t)21 * N + s] = lF[2];
         }
     } else {
         dkf = dkg = domf = 0.f;
@@ -353,6 +369,7 @@ static void fill_adj(dl_handle* h, AdjArgs& a) {
     a.grads = h->adj_grads;
     a.aux = h->adj_aux;
     a.les = P.les ? 1 : 0;
+    a.spec = h->force_mode == DL_FORCE_SPECTRAL ? 1 : 0;
     a.csd = (float)(P.Cs * P.Cs * P.delta * P.delta);
     a.nu1 = (float)P.nu1;
     a.inv_ds = (float)(1.0 / P.ds);
@@ -363,7 +380,8 @@ int adjoint_check(dl_handle* h) {
         return set_error(h, DL_ERR_UNSUPPORTED, "the adjoint is implemented for the two-phase FP32 form");
     if (h->P.les && h->P.Anu != 0.0) return set_error(h, DL_ERR_UNSUPPORTED, "the adjoint assumes A_nu = 0");
     if (h->P.nu2 != h->P.nu1) return set_error(h, DL_ERR_UNSUPPORTED, "the adjoint assumes viscosity ratio 1");
-    if (h->force_mode == DL_FORCE_SPECTRAL) return set_error(h, DL_ERR_UNSUPPORTED, "the adjoint covers no spectral force");
+    if (h->force_mode == DL_FORCE_SPECTRAL && h->sp.K < 1)
+        return set_error(h, DL_ERR_UNSUPPORTED, "the adjoint of the spectral force needs the band plan");
     if (h->P.wall_u[1] != 0.0 || h->P.wall_u[2] != 0.0)
         return set_error(h, DL_ERR_UNSUPPORTED, "the adjoint assumes an x wall velocity");
     if (!h->adj_lam[0]) {
@@ -420,6 +438,14 @@ int adjoint_step(dl_handle* h, const float* d_state, long long step) {
         DL_LAUNCH(h, false, (adj_walls<<<nb(2 * plane), 256, 0, h->stream>>>(w)));
     }
     DL_LAUNCH(h, true, (adj_local<<<nb(h->N), 256, 0, h->stream>>>(a)));
+    if (a.spec) {
+        const size_t N = h->N;
+        float* x = h->adj_aux;
+        const float* m = a.mac;
+        rc = spectral_adjoint_f32(h, x + 19 * N, x + 20 * N, x + 21 * N, m + N, m + 2 * N, m + 3 * N, x + 6 * N,
+                                  x + 7 * N, x + 8 * N);
+        if (rc != DL_OK) return rc;
+    }
     DL_LAUNCH(h, false, (adj_stencil<<<nb(h->N), 256, 0, h->stream>>>(a, nullptr)));
     DL_CUDA(h, cudaGetLastError());
     h->adj_cur = 1 - h->adj_cur;

@@ -305,6 +305,8 @@ int dl_load_state(dl_handle* h, const void* d_src) {
     h->fields_set = true;
     h->eq_init = true;
     h->pushed = 0;
+    // the band coefficients of the next step come from the loaded u
+    if (h->force_mode == DL_FORCE_SPECTRAL) h->fsp.dirty = 1;
     return DL_OK;
 }
 
@@ -541,6 +543,8 @@ int dl_set_force(dl_handle* h, int mode, const double* fx, const double* fy, con
         return set_error(h, DL_ERR_ARG,
                          "spectral forcing needs kc >= 2 and a domain holding the band (2 kc - 1 <= nx, ny; "
                          "kc <= nz / 2)");
+    if (is_fast(h) && mode != DL_FORCE_NONE && h->P.ds != 1.0)
+        return set_error(h, DL_ERR_UNSUPPORTED, "the FP32 and FP16 forms apply a body force at ds = 1 only");
     if (is_fast(h)) {
         int rc = fast_prepare_force(h, mode);
         if (rc != DL_OK) return rc;

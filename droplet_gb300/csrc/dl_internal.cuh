@@ -88,6 +88,7 @@ struct SpectralPlan {
     double* d_uh;     // [3][2K+1][2K+1][K+1] complex (band coefficients, /N)
     double* d_b2;     // [3][2K+1][ny*nz] complex   (synthesis, x pending)
     float* d_twxf;    // FP32 copy of d_twx
+    double* d_lh;     // adjoint: band coefficients of dL/dF, as d_uh (allocated on first use)
 };
 
 // In-kernel band forcing of the FP32 / FP16 forms.
@@ -214,6 +215,8 @@ int push_step(dl_handle* h);
 int fast_settle(dl_handle* h);  // complete a push step's state (no-op when settled)
 int fast_prepare_force(dl_handle* h, int mode);
 int spectral_project_f32(dl_handle* h, const float* d_u1, const float* d_u2, const float* d_u3);
+int spectral_adjoint_f32(dl_handle* h, const float* d_lf1, const float* d_lf2, const float* d_lf3, const float* d_u1,
+                         const float* d_u2, const float* d_u3, float* d_lu1, float* d_lu2, float* d_lu3);
 // batched ensembles of fast-form handles (step_fast.cu)
 int batch_create(dl_handle** members, int nm, void** out);
 void batch_destroy(void* b);

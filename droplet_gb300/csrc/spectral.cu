@@ -295,6 +295,67 @@ __global__ void sp_synth_x_f32(const double* __restrict__ b2, float* __restrict_
     fz[s] = out[2];
 }
 
+// ---- adjoint of the band force (reverse pass of a step with the spectral force) ----
+// F = coef v with v = P u, the band-pass of u (sum over the band of w Re(u_hat
+// e^{ik.x}), u_hat = DFT(u)/N), coef = 0.5 eps / E and E = sum w 0.5 |u_hat|^2 =
+// |v|^2 / 2N. For lF = dL/dF, since P is a symmetric projection and dE/du = v/N:
+//   dL/du = coef P lF - (s coef / (E N)) v,   s = sum_x lF . v = N sum w Re(u_hat conj(L_hat)),
+// with L_hat the band coefficients of lF: one synthesis of the combined
+// coefficients coef L_hat - (s coef / (E N)) u_hat. One block; reads E and coef
+// that sp_energy left, writes the combination into uh and sets coef = 1 for
+// the synthesis kernels.
+__global__ void sp_adj_combine(const SpArgs a, const double* __restrict__ lh) {
+    __shared__ double s_part[32];
+    const int NK = 2 * a.K + 1;
+    const int nv = 3 * NK * NK * (a.K + 1);
+    const double E = a.st->sp_energy, coef = a.st->sp_coef;
+    double s = 0.0;
+    for (int t = threadIdx.x; t < nv; t += blockDim.x) {
+        const int kz = t % (a.K + 1), r = t / (a.K + 1), kyi = r % NK, kxi = (r / NK) % NK;
+        const int kx = kxi - a.K, ky = kyi - a.K, kk = kx * kx + ky * ky + kz * kz;
+        if (kk < 1 || kk >= a.kc2) continue;
+        const double w = kz == 0 ? 1.0 : 2.0;
+        s += w * (a.uh[2 * t] * lh[2 * t] + a.uh[2 * t + 1] * lh[2 * t + 1]);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) s_part[threadIdx.x >> 5] = s;
+    __syncthreads();
+    double tot = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += s_part[w];
+    const double g = tot * coef / E;  // s coef / (E N), s = N tot
+    for (int t = threadIdx.x; t < 2 * nv; t += blockDim.x) a.uh[t] = coef * lh[t] - g * a.uh[t];
+    __syncthreads();
+    if (threadIdx.x == 0) a.st->sp_coef = 1.0;
+}
+
+// the x synthesis added into FP32 arrays
+__global__ void sp_synth_x_add_f32(const double* __restrict__ b2, float* __restrict__ o1, float* __restrict__ o2,
+                                   float* __restrict__ o3, int nx, int ny, int nz, int K,
+                                   const float* __restrict__ tw) {
+    const long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long N = (long long)nx * ny * nz;
+    if (s >= N) return;
+    const int x = (int)(s % nx);
+    const long long r = s / nx;
+    const int y = (int)(r % ny), z = (int)(r / ny);
+    const int NK = 2 * K + 1;
+    float out[3] = {0.f, 0.f, 0.f};
+    for (int k = 0; k < NK; ++k) {
+        int m = ((k - K) * x) % nx;
+        m = m < 0 ? m + nx : m;
+        const float cs = tw[2 * m], sn = tw[2 * m + 1];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const double* v = b2 + 2 * ((((long long)c * NK + k) * ny + y) * nz + z);
+            out[c] += (float)v[0] * cs - (float)v[1] * sn;
+        }
+    }
+    o1[s] += out[0];
+    o2[s] += out[1];
+    o3[s] += out[2];
+}
+
 static int upload_twiddle(dl_handle* h, int n, double** d) {
     std::vector<double> t(2 * (size_t)n);
     const double pi = acos(-1.0);
@@ -360,6 +421,7 @@ void spectral_free(dl_handle* h) {
     cudaFree(sp.d_b2);
     cudaFree(sp.d_uh);
     cudaFree(sp.d_twxf);
+    cudaFree(sp.d_lh);
     memset(&sp, 0, sizeof(sp));
 }
 
@@ -422,6 +484,34 @@ int spectral_project_f32(dl_handle* h, const float* u1, const float* u2, const f
                                                                         h->sp.d_twxf));
     DL_LAUNCH(h, false, sp_ystage<<<nb(3LL * NK * NK * h->nz, 128), 128, 0, s>>>(a));
     DL_LAUNCH(h, false, sp_zstage<<<nb(3LL * NK * NK * (a.K + 1), 64), 64, 0, s>>>(a));
+    DL_CUDA(h, cudaGetLastError());
+    return DL_OK;
+}
+
+// dL/du of the band force added into lu, from dL/dF (lf) and the u the force was
+// computed from
+int spectral_adjoint_f32(dl_handle* h, const float* lf1, const float* lf2, const float* lf3, const float* u1,
+                         const float* u2, const float* u3, float* lu1, float* lu2, float* lu3) {
+    SpectralPlan& sp = h->sp;
+    if (sp.K < 1) return set_error(h, DL_ERR_STATE, "no band plan for the spectral force");
+    const int NK = 2 * sp.K + 1;
+    const size_t nuh = (size_t)2 * 3 * NK * NK * (sp.K + 1);
+    if (!sp.d_lh) DL_CUDA(h, cudaMalloc(&sp.d_lh, sizeof(double) * nuh));
+    int rc = spectral_project_f32(h, lf1, lf2, lf3);
+    if (rc != DL_OK) return rc;
+    DL_CUDA(h, cudaMemcpyAsync(sp.d_lh, sp.d_uh, sizeof(double) * nuh, cudaMemcpyDeviceToDevice, h->stream));
+    rc = spectral_project_f32(h, u1, u2, u3);
+    if (rc != DL_OK) return rc;
+    SpArgs a;
+    fill_sp(h, a);
+    cudaStream_t s = h->stream;
+    const long long N = (long long)h->N;
+    DL_LAUNCH(h, false, sp_energy<<<1, 32, 0, s>>>(a));
+    DL_LAUNCH(h, false, sp_adj_combine<<<1, 256, 0, s>>>(a, sp.d_lh));
+    DL_LAUNCH(h, false, sp_synth_z<<<nb(3LL * NK * NK * h->nz, 128), 128, 0, s>>>(a));
+    DL_LAUNCH(h, false, sp_synth_y<<<nb(3LL * NK * h->ny * h->nz, 128), 128, 0, s>>>(a));
+    DL_LAUNCH(h, false, sp_synth_x_add_f32<<<nb(N, 256), 256, 0, s>>>(a.b2, lu1, lu2, lu3, h->nx, h->ny, h->nz, a.K,
+                                                                       sp.d_twxf));
     DL_CUDA(h, cudaGetLastError());
     return DL_OK;
 }

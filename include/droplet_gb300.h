@@ -334,8 +334,9 @@ int dl_label_droplets(dl_handle* h, int connectivity, int32_t* labels, int64_t* 
  * checkpointing: save states with dl_save_state (device memory of
  * dl_state_floats floats), recompute segments with dl_load_state + dl_step,
  * and walk them backwards with dl_adjoint_step. It covers the shear-droplet
- * physics (walls, static force, viscosity ratio 1) and the Smagorinsky eddy
- * viscosity (LES, A_nu = 0); no spectral force. */
+ * physics (walls, static force, viscosity ratio 1), the Smagorinsky eddy
+ * viscosity (LES, A_nu = 0) and the band force (DL_FORCE_SPECTRAL), i.e. the
+ * forced-turbulence step of program/lbm_drop_iht_xy.f90:1016-1026. */
 
 /* Number of FP32 values of one full device state (populations and fields;
  * dl_save_state / dl_load_state / dl_adjoint_init). */

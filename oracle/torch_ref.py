@@ -86,16 +86,43 @@ def les_taug(P, u):
     return 0.5 + 3.0 * (P.nu1 + nut) / P.ds
 
 
-def step(P, f, g, kf, kg, tauf, U, taug):
+def band_force(P, u):
+    """Constant-injection band forcing (program/lbm_drop_iht_xy.f90:722-842):
+    u_hat = FFT(u)/N on the band 1 <= |k|^2 < kc^2, E = sum 0.5 |u_hat|^2 over
+    the band (the full spectrum, which the reference's half spectrum with
+    weights min(2, k3+1) equals), F = (0.5 eps / E) times the band-passed u."""
+    nz, ny, nx = u[0].shape
+    N = nx * ny * nz
+    kz = torch.fft.fftfreq(nz, d=1.0 / nz).view(nz, 1, 1)
+    ky = torch.fft.fftfreq(ny, d=1.0 / ny).view(1, ny, 1)
+    kx = torch.fft.fftfreq(nx, d=1.0 / nx).view(1, 1, nx)
+    kk = kx * kx + ky * ky + kz * kz
+    mask = ((kk >= 1) & (kk < P.kc * P.kc)).to(torch.float64)
+    uh = [torch.fft.fftn(c) / N * mask for c in u]
+    E = 0.5 * sum((h.real ** 2 + h.imag ** 2).sum() for h in uh)
+    coef = 0.5 * P.eps / E
+    return [coef * torch.fft.ifftn(h).real * N for h in uh]
+
+
+def step(P, f, g, kf, kg, tauf, U, taug, spectral=False):
     """One time step at viscosity ratio 1: tau_g constant, or from the
-    Smagorinsky strain when P.les. U: top-wall x velocity (tensor); the
-    bottom wall moves with -U."""
+    Smagorinsky strain when P.les; with spectral, the band force of the
+    step's u at the source. U: top-wall x velocity (tensor); the bottom wall
+    moves with -U. spectral="frozen" applies the force with no gradient
+    through it (tests use it to show that its adjoint matters)."""
     phi, u, p = moments(f, g)
     feq, geq = equilibria(P, phi, u, p, kf, kg)
     if P.les:
         taug = les_taug(P, u)
     fn = [nb(f[i] - (f[i] - feq[i]) / tauf, i, -1) for i in range(15)]
-    gn = [nb(g[i] - (g[i] - geq[i]) / taug, i, -1) for i in range(15)]
+    if spectral:
+        F = band_force(P, u)
+        if spectral == "frozen":
+            F = [c.detach() for c in F]
+        gn = [nb(g[i] - (g[i] - geq[i]) / taug + 3.0 * P.ds * E[i] * (CX[i] * F[0] + CY[i] * F[1] + CZ[i] * F[2]),
+                 i, -1) for i in range(15)]
+    else:
+        gn = [nb(g[i] - (g[i] - geq[i]) / taug, i, -1) for i in range(15)]
     if P.walls:
         Uv = (U, 0.0, 0.0)
         gb = list(gn)
@@ -126,11 +153,11 @@ def deformation(P, phi):
     return (a - b) / (a + b)
 
 
-def run_loss(P, phi0, u0, p0, kf, kg, tauf, U, taug, nsteps):
+def run_loss(P, phi0, u0, p0, kf, kg, tauf, U, taug, nsteps, spectral=False):
     """Initialise at equilibrium from (phi0, u0, p0) and return D after nsteps."""
     feq, geq = equilibria(P, phi0, u0, p0, kf, kg)
     f, g = feq, geq
     for _ in range(nsteps):
-        f, g = step(P, f, g, kf, kg, tauf, U, taug)
+        f, g = step(P, f, g, kf, kg, tauf, U, taug, spectral)
     phi, _, _ = moments(f, g)
     return deformation(P, phi)
