@@ -80,8 +80,8 @@ def deformation_from_diag(d: dict, phi1: float, phi2: float):
 class CheckpointedRun:
     """Forward and reverse passes of one FP32 run. When the per-step adjoint
     states of the whole run fit in `memory_fraction` of the free device memory
-    (20 FP32 values per site and step, 35 with LES; 35 GB for 500 steps of
-    96^3 without), the
+    (20 FP32 values per site and step, 35 with LES or a viscosity ratio; 35 GB
+    for 500 steps of 96^3 with 20), the
     forward keeps all of them and the reverse pass recomputes nothing;
     otherwise it keeps a full state every S = ceil(sqrt(n)) steps and
     recomputes each segment once. The loss and its gradient stay on the
@@ -105,7 +105,7 @@ class CheckpointedRun:
         self.store_all = False
         if segment is None:
             nx, ny, nz = self.shape
-            need = self.nsteps * (35 if params.les else 20) * nx * ny * nz * 4
+            need = self.nsteps * (35 if (params.les or params.nu2 != params.nu1) else 20) * nx * ny * nz * 4
             free, _ = torch.cuda.mem_get_info()
             self.store_all = need <= memory_fraction * free
             segment = self.nsteps if self.store_all else max(1, math.ceil(math.sqrt(self.nsteps)))

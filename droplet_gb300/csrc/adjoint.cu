@@ -4,7 +4,7 @@
 //
 // Forward step being differentiated (program/lbm_drop_xy.f90:421-588 with the
 // walls of prototype_program/two-phase/drop8_mpi.f90:642-674), at constant
-// tau_g (viscosity ratio 1):
+// tau_g (viscosity ratio 1; see below for the per-site tau_g):
 //   f'_i(x) = (1 - wf) f_i(x - c_i) + wf feq_i(x - c_i)
 //   g'_i(x) = (1 - wg) g_i(x - c_i) + wg geq_i(x - c_i)   (+ a constant force)
 //   wall nodes: g'_i = g'_j - 6 E_j (U_wall . c_j) for the reflected pairs
@@ -17,7 +17,10 @@
 // per site: tau_g = 1/2 + 3 (nu + nu_t)/ds, nu_t = csd sqrt(2 S:S), S the
 // symmetric part of G_ab = d u_a / d x_b from the 14-neighbour stencil of u;
 // its adjoint needs the pre-step g (the adjoint state then carries it) and
-// sends dL/dG back to u through the transposed stencil. With the band force
+// sends dL/dG back to u through the transposed stencil. With a viscosity ratio
+// other than 1 in the fixed-range mode (program/lbm_drop_xy.f90:254-285),
+// nu = nu1 + (phi - phi1) (nu2 - nu1) / (phi2 - phi1) makes wg a function of
+// the site's phi as well; dL/dwg then also reaches phi. With the band force
 // (program/lbm_drop_iht_xy.f90:722-842), g'_i(x) gains 3 E_i c_i . F(x - c_i),
 // F = (0.5 eps / E(u)) P u from the band projection P of the pre-step u:
 // adj_local forms dL/dF(y) = sum_i 3 E_i c_i b_i(y) and spectral_adjoint_f32
@@ -59,10 +62,11 @@ struct AdjArgs {
     int walls_on;             // the walls moved in this step
     int stream;               // 1: a time step; 0: the initial f = feq, g = geq
     int les;                  // Smagorinsky eddy viscosity in tau_g (time steps)
+    float kvis;               // d nu / d phi: (nu2 - nu1) / (phi2 - phi1) (fixed range), 0 at ratio 1
     int spec;                 // band force (time steps): aux rows 19..21 receive dL/dF
     float csd, nu1, inv_ds;   // LES: (Cs delta)^2, nu, 1/ds
 };
-constexpr int ADJ_AUX = 22;  // aux rows: 9, LES 10 more (9 .. 18), band force 3 more (19 .. 21)
+constexpr int ADJ_AUX = 22;  // aux rows: 9, LES dL/dG (9 .. 17), per-site wg (18), band force dL/dF (19 .. 21)
 
 constexpr int ADJ_NREP = 64;  // copies of the gradient accumulators (spreads the atomics)
 
@@ -155,10 +159,11 @@ __global__ void __launch_bounds__(256) adj_local(AdjArgs a) {
     const float p0ref = a.phi1 * a.T / (1.f - a.b * a.phi1) - a.a * a.phi1 * a.phi1;
     const float dp0 = a.T / (omb * omb) - 2.f * a.a * phi;
     const float dA = (p0 - p0ref) - a.kf * phi * lap - a.kf6 * gsq;
-    // LES: G_ab = d u_a / d x_b, S, nu_t, wg of this site
+    // per-site wg (LES and / or a viscosity ratio): G_ab = d u_a / d x_b, S, nu_t, nu(phi)
     const bool les = a.les && a.stream;
+    const bool pw = (a.les || a.kvis != 0.f) && a.stream;
     float G[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
-    float tt = 0.f, wgs = a.omg;
+    float tt = 0.f, wgs = a.omg, nut = 0.f;
     if (les) {
 #pragma unroll
         for (int k = 1; k < Q; ++k) {
@@ -186,10 +191,10 @@ __global__ void __launch_bounds__(256) adj_local(AdjArgs a) {
                 acc += sab * sab;
             }
         tt = 2.f * acc;
-        const float nut = tt > 0.f ? a.csd * sqrtf(tt) : 0.f;
-        wgs = 1.f / (0.5f + 3.f * (a.nu1 + nut) * a.inv_ds);
+        nut = tt > 0.f ? a.csd * sqrtf(tt) : 0.f;
     }
-    float lw = 0.f;  // LES: dL/dwg of this site
+    if (pw) wgs = 1.f / (0.5f + 3.f * (a.nu1 + dphi * a.kvis + nut) * a.inv_ds);
+    float lw = 0.f;  // per-site wg: dL/dwg of this site
     float lF[3] = {0.f, 0.f, 0.f};  // band force: dL/dF of this site
     float lphi = 0.f, lA = 0.f, lp = 0.f, lusq = 0.f, lgsq = 0.f;
     float lu[3] = {0.f, 0.f, 0.f}, lgr[3] = {0.f, 0.f, 0.f};
@@ -217,7 +222,7 @@ __global__ void __launch_bounds__(256) adj_local(AdjArgs a) {
             lF[1] += 3.f * E * cy(i) * bi;
             lF[2] += 3.f * E * cz(i) * bi;
         }
-        if (les) {  // geq_i - g_i in deviations (the bulk E_i cancels)
+        if (pw) {  // geq_i - g_i in deviations (the bulk E_i cancels)
             const float dgeq = E * (3.f * dp + 3.f * cu + 4.5f * cu * cu - 1.5f * usq + a.kg * cGc);
             lw += bi * (dgeq - a.gst[(size_t)i * N + s]);
         }
@@ -243,6 +248,8 @@ __global__ void __launch_bounds__(256) adj_local(AdjArgs a) {
     lu[2] += 2.f * u3 * lusq;
     dkf += lA * (-phi * lap - gsq / 6.f);
     lphi += lA * (dp0 - a.kf * lap);
+    const float lnu = pw ? lw * (-3.f * wgs * wgs * a.inv_ds) : 0.f;  // dL/dnu (and dL/dnu_t)
+    lphi += lnu * a.kvis;
     const float llap = -a.kf * phi * lA;
     lgsq -= a.kf6 * lA;
     lgr[0] += 2.f * gr[0] * lgsq;
@@ -260,14 +267,14 @@ __global__ void __launch_bounds__(256) adj_local(AdjArgs a) {
         a.aux[8 * N + s] = lu[2];
         if (a.les) {
             // dwg/dnu_t = -3 wg^2 / ds, dnu_t/dtt = csd / (2 sqrt(tt)), dtt/dG_ab = 4 S_ab
-            const float ltt = (les && tt > 0.f) ? lw * (-3.f * wgs * wgs * a.inv_ds) * (0.5f * a.csd / sqrtf(tt)) : 0.f;
+            const float ltt = (les && tt > 0.f) ? lnu * (0.5f * a.csd / sqrtf(tt)) : 0.f;
 #pragma unroll
             for (int al = 0; al < 3; ++al)
 #pragma unroll
                 for (int be = 0; be < 3; ++be)
                     a.aux[(size_t)(9 + al + 3 * be) * N + s] = ltt * 2.f * (G[al][be] + G[be][al]);
-            a.aux[(size_t)18 * N + s] = wg;
         }
+        if (a.les || a.kvis != 0.f) a.aux[(size_t)18 * N + s] = wg;
         if (a.spec) {
             a.aux[(size_t)19 * N + s] = lF[0];
             a.aux[(size_t)20 * N + s] = lF[1];
@@ -317,8 +324,8 @@ __global__ void __launch_bounds__(256) adj_stencil(AdjArgs a, float* phi_out) {
         lu1 += a.inv_grad * t[0];
         lu2 += a.inv_grad * t[1];
         lu3 += a.inv_grad * t[2];
-        wg = a.aux[(size_t)18 * N + s];
     }
+    if ((a.les || a.kvis != 0.f) && a.stream) wg = a.aux[(size_t)18 * N + s];
     if (phi_out) phi_out[s] = lphi;
     // the streamed part (1 - w) of the collision, gathered here rather than
     // stored by adj_local and read back
@@ -369,6 +376,7 @@ static void fill_adj(dl_handle* h, AdjArgs& a) {
     a.grads = h->adj_grads;
     a.aux = h->adj_aux;
     a.les = P.les ? 1 : 0;
+    a.kvis = (float)((P.nu2 - P.nu1) / (P.phi2 - P.phi1));
     a.spec = h->force_mode == DL_FORCE_SPECTRAL ? 1 : 0;
     a.csd = (float)(P.Cs * P.Cs * P.delta * P.delta);
     a.nu1 = (float)P.nu1;
@@ -379,7 +387,10 @@ int adjoint_check(dl_handle* h) {
     if (h->form != DL_FORM_FP32 || h->single)
         return set_error(h, DL_ERR_UNSUPPORTED, "the adjoint is implemented for the two-phase FP32 form");
     if (h->P.les && h->P.Anu != 0.0) return set_error(h, DL_ERR_UNSUPPORTED, "the adjoint assumes A_nu = 0");
-    if (h->P.nu2 != h->P.nu1) return set_error(h, DL_ERR_UNSUPPORTED, "the adjoint assumes viscosity ratio 1");
+    if (h->P.nu2 != h->P.nu1 && h->P.visc_mode != DL_VISC_FIXED)
+        return set_error(h, DL_ERR_UNSUPPORTED,
+                         "a viscosity ratio other than 1 needs the fixed-range mode (the global phi range has no "
+                         "adjoint here)");
     if (h->force_mode == DL_FORCE_SPECTRAL && h->sp.K < 1)
         return set_error(h, DL_ERR_UNSUPPORTED, "the adjoint of the spectral force needs the band plan");
     if (h->P.wall_u[1] != 0.0 || h->P.wall_u[2] != 0.0)

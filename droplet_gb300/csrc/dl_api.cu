@@ -314,7 +314,8 @@ int dl_adjoint_state_floats(dl_handle* h, int64_t* n) {
     if (!h || !n) return DL_ERR_ARG;
     if (h->form != DL_FORM_FP32 || h->single)
         return set_error(h, DL_ERR_UNSUPPORTED, "device state export is for the two-phase FP32 form");
-    *n = (int64_t)(h->P.les ? 35 : 20) * (int64_t)h->N;  // f, fields (, g: the Smagorinsky adjoint reads it)
+    // f, fields (, g: the adjoint of a per-site tau_g, LES or a viscosity ratio, reads it)
+    *n = (int64_t)((h->P.les || h->P.nu2 != h->P.nu1) ? 35 : 20) * (int64_t)h->N;
     return DL_OK;
 }
 
@@ -331,7 +332,7 @@ int dl_save_adjoint_state(dl_handle* h, void* d_dst) {
     DL_CUDA(h, cudaMemcpyAsync(d, h->fs[h->cur], sizeof(float) * Q * N, cudaMemcpyDeviceToDevice, h->stream));
     DL_CUDA(h, cudaMemcpyAsync(d + Q * N, h->mac32[h->cur], sizeof(float) * 5 * N, cudaMemcpyDeviceToDevice,
                                h->stream));
-    if (h->P.les)
+    if (h->P.les || h->P.nu2 != h->P.nu1)
         DL_CUDA(h, cudaMemcpyAsync(d + 20 * N, h->gs[h->cur], sizeof(float) * Q * N, cudaMemcpyDeviceToDevice,
                                    h->stream));
     return DL_OK;

@@ -334,9 +334,10 @@ int dl_label_droplets(dl_handle* h, int connectivity, int32_t* labels, int64_t* 
  * checkpointing: save states with dl_save_state (device memory of
  * dl_state_floats floats), recompute segments with dl_load_state + dl_step,
  * and walk them backwards with dl_adjoint_step. It covers the shear-droplet
- * physics (walls, static force, viscosity ratio 1), the Smagorinsky eddy
- * viscosity (LES, A_nu = 0) and the band force (DL_FORCE_SPECTRAL), i.e. the
- * forced-turbulence step of program/lbm_drop_iht_xy.f90:1016-1026. */
+ * physics (walls, static force; viscosity ratio 1, or another ratio in the
+ * DL_VISC_FIXED mode), the Smagorinsky eddy viscosity (LES, A_nu = 0) and the
+ * band force (DL_FORCE_SPECTRAL), i.e. the forced-turbulence step of
+ * program/lbm_drop_iht_xy.f90:1016-1026. */
 
 /* Number of FP32 values of one full device state (populations and fields;
  * dl_save_state / dl_load_state / dl_adjoint_init). */
@@ -350,8 +351,8 @@ int dl_load_state(dl_handle* h, const void* d_src);
 int dl_adjoint_begin(dl_handle* h, const float* d_dloss_dphi);
 
 /* The part of a state that the reverse of one step reads (f and the fields,
- * and with LES g as well: dl_adjoint_state_floats FP32 values, 20 or 35 per
- * site): what the recomputed segment keeps per step, written by
+ * and with LES or a viscosity ratio g as well: dl_adjoint_state_floats FP32
+ * values, 20 or 35 per site): what the recomputed segment keeps per step, written by
  * dl_save_adjoint_state. */
 int dl_adjoint_state_floats(dl_handle* h, int64_t* n);
 int dl_save_adjoint_state(dl_handle* h, void* d_dst);

@@ -4,7 +4,7 @@ Used as the "plain PyTorch autodiff reference" for the hand-written adjoint:
 the same physics as the C oracle (program/lbm_drop_xy.f90:421-666 with the
 moving-wall bounce-back of prototype_program/two-phase/drop8_mpi.f90:642-674
 and, when P.les, the Smagorinsky tau_g of program/LES_drop_xy.f90:481-502,
-663-690),
+663-690; a viscosity ratio in the fixed-range mode),
 written with torch.roll so that autograd differentiates it, in FP64. It does
 not follow the reference's evaluation order (it is not a parity restatement);
 its job is gradients.
@@ -66,6 +66,18 @@ def moments(f, g):
     return phi, u, p
 
 
+def taug_field(P, phi, u, frozen_visc=False):
+    """tau_g = 1/2 + 3 (nu(phi) + nu_t)/ds: nu(phi) = nu1 + (phi - phi1)(nu2 -
+    nu1)/(phi2 - phi1) (the fixed-range mode, program/lbm_drop_xy.f90:254-285),
+    nu_t the Smagorinsky term when P.les. frozen_visc: no gradient through
+    nu(phi) (tests use it to show that its adjoint matters)."""
+    ph = phi.detach() if frozen_visc else phi
+    nu = P.nu1 + (ph - P.phi1) / (P.phi2 - P.phi1) * (P.nu2 - P.nu1)
+    if P.les:
+        nu = nu + (les_taug(P, u) - 0.5) * P.ds / 3.0 - P.nu1
+    return 0.5 + 3.0 * nu / P.ds
+
+
 def les_taug(P, u):
     """tau_g = 1/2 + 3 (nu1 + nu_t)/ds, nu_t = (Cs delta)^2 sqrt(2 S:S), S the
     symmetric part of d u_a / d x_b from the 14-neighbour stencil."""
@@ -104,7 +116,7 @@ def band_force(P, u):
     return [coef * torch.fft.ifftn(h).real * N for h in uh]
 
 
-def step(P, f, g, kf, kg, tauf, U, taug, spectral=False):
+def step(P, f, g, kf, kg, tauf, U, taug, spectral=False, frozen_visc=False):
     """One time step at viscosity ratio 1: tau_g constant, or from the
     Smagorinsky strain when P.les; with spectral, the band force of the
     step's u at the source. U: top-wall x velocity (tensor); the bottom wall
@@ -112,8 +124,8 @@ def step(P, f, g, kf, kg, tauf, U, taug, spectral=False):
     through it (tests use it to show that its adjoint matters)."""
     phi, u, p = moments(f, g)
     feq, geq = equilibria(P, phi, u, p, kf, kg)
-    if P.les:
-        taug = les_taug(P, u)
+    if P.les or P.nu2 != P.nu1:
+        taug = taug_field(P, phi, u, frozen_visc)
     fn = [nb(f[i] - (f[i] - feq[i]) / tauf, i, -1) for i in range(15)]
     if spectral:
         F = band_force(P, u)
@@ -153,11 +165,11 @@ def deformation(P, phi):
     return (a - b) / (a + b)
 
 
-def run_loss(P, phi0, u0, p0, kf, kg, tauf, U, taug, nsteps, spectral=False):
+def run_loss(P, phi0, u0, p0, kf, kg, tauf, U, taug, nsteps, spectral=False, frozen_visc=False):
     """Initialise at equilibrium from (phi0, u0, p0) and return D after nsteps."""
     feq, geq = equilibria(P, phi0, u0, p0, kf, kg)
     f, g = feq, geq
     for _ in range(nsteps):
-        f, g = step(P, f, g, kf, kg, tauf, U, taug, spectral)
+        f, g = step(P, f, g, kf, kg, tauf, U, taug, spectral, frozen_visc)
     phi, _, _ = moments(f, g)
     return deformation(P, phi)

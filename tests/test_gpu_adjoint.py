@@ -124,14 +124,14 @@ def case_les():
     return w
 
 
-def torch_grads(P, f, nsteps, les, spectral=False):
+def torch_grads(P, f, nsteps, les, spectral=False, frozen_visc=False):
     T = lambda a: torch.tensor(a, dtype=torch.float64)  # noqa: E731
     phi0 = T(f["phi"]).requires_grad_(True)
     ps = [torch.tensor(v, dtype=torch.float64, requires_grad=True)
           for v in (P.kappaf, P.kappag, P.tauf, P.wall_u[0])]
     taug = 0.5 + 3.0 * P.nu1 / P.ds
     L = torch_ref.run_loss(P.replace(les=1 if les else 0), phi0, [T(f["u1"]), T(f["u2"]), T(f["u3"])], T(f["p"]),
-                           *ps, taug, nsteps, spectral)
+                           *ps, taug, nsteps, spectral, frozen_visc)
     L.backward()
     # (no walls: U takes no part and has no gradient)
     out = {k: (p.grad.item() if p.grad is not None else 0.0) for k, p in zip(("dkappaf", "dkappag", "dtauf", "dU"), ps)}
@@ -223,4 +223,46 @@ def test_adjoint_band_force_matches_fp64_finite_differences(adjoint_spectral):
         h = 1e-4 * abs(base)
         fd = (fp64_loss(mk(h), w, SPEC_STEPS, _abi.DL_FORCE_SPECTRAL) -
               fp64_loss(mk(-h), w, SPEC_STEPS, _abi.DL_FORCE_SPECTRAL)) / (2 * h)
+        assert abs(g[name] - fd) <= 2e-2 * abs(fd) + 1e-12, (name, g[name], fd)
+
+
+VISC_STEPS = 60
+
+
+@pytest.fixture(scope="module")
+def adjoint_visc():
+    """The shear droplet with viscosity ratio 3 (nu2 = 3 nu1) in the
+    fixed-range mode: tau_g follows the site's phi."""
+    w = configs.shear_droplet(n=32, radius=6.0, U=0.04, steps=VISC_STEPS, form=32)
+    w.params = w.params.replace(nu2=3.0 * w.params.nu1, visc_mode=_abi.DL_VISC_FIXED)
+    f = w.fields
+    run = CheckpointedRun(w.params, w.shape, (f["u1"], f["u2"], f["u3"]), f["p"], VISC_STEPS)
+    D = run.forward(f["phi"])
+    g = run.backward()
+    run.close()
+    return w, D, g, torch_grads(w.params, f, VISC_STEPS, False)
+
+
+def test_adjoint_viscosity_ratio_matches_torch_autodiff(adjoint_visc):
+    w, D, g, ref = adjoint_visc
+    assert abs(ref["D"] - D) <= 1e-4 * abs(ref["D"])
+    errs = {k: abs(g[k] - ref[k]) / abs(ref[k]) for k in ("dkappaf", "dkappag", "dtauf", "dU")}
+    errs["dphi0"] = np.linalg.norm(g["dphi0"] - ref["dphi0"]) / np.linalg.norm(ref["dphi0"])
+    frozen = torch_grads(w.params, w.fields, VISC_STEPS, False, frozen_visc=True)
+    off = {k: abs(frozen[k] - ref[k]) / abs(ref[k]) for k in ("dkappaf", "dkappag", "dtauf", "dU")}
+    off["dphi0"] = np.linalg.norm(frozen["dphi0"] - ref["dphi0"]) / np.linalg.norm(ref["dphi0"])
+    print("viscosity-ratio adjoint: relative error", errs, "frozen-nu(phi) reference off by", off)
+    for k in ("dkappaf", "dkappag", "dtauf", "dU"):
+        assert errs[k] <= 2e-2, (k, g[k], ref[k])
+    assert errs["dphi0"] <= 5e-2, errs
+    assert max(off.values()) > 5e-2, off
+
+
+def test_adjoint_viscosity_ratio_matches_fp64_finite_differences(adjoint_visc):
+    w, D, g, _ = adjoint_visc
+    P = w.params
+    for name, mk, base in (("dkappag", lambda h: P.replace(kappag=P.kappag + h), P.kappag),
+                           ("dU", lambda h: P.replace(wall_u=(P.wall_u[0] + h, 0.0, 0.0)), P.wall_u[0])):
+        h = 1e-4 * abs(base)
+        fd = (fp64_loss(mk(h), w, VISC_STEPS) - fp64_loss(mk(-h), w, VISC_STEPS)) / (2 * h)
         assert abs(g[name] - fd) <= 2e-2 * abs(fd) + 1e-12, (name, g[name], fd)
