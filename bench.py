@@ -704,30 +704,40 @@ def measure_ensemble(n_members: int, steps: int, form: int, stream, tune: bool =
 
     ws = configs.ensemble_members(n_members=n_members, form=form)
     sites = sum(w.n_sites for w in ws)
-    ens = Ensemble([w.params for w in ws], [w.shape for w in ws], form)
-    ens.set_stream(stream.cuda_stream)
-    for mem, w in zip(ens.members, ws):
-        mem.set_fields(**w.fields)
-        mem.init_equilibrium()
-        mem.set_force(w.force_mode)
-    persistent = int(ens.get_option("persistent"))
-    tuned = autotune.tune_ensemble(ens) if tune else {"lz": int(ens.get_option("lz"))}
-    ens.step(4)
-    ens.sync()
-    ens.profile(True, every=EVENT_STRIDE)
-    torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    ens.step(steps)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1)
-    prof = ens.profile_read()
-    ens.profile(False)
-    ens.sync()
+
+    def timed(persistent):
+        ens = Ensemble([w.params for w in ws], [w.shape for w in ws], form)
+        ens.set_stream(stream.cuda_stream)
+        for mem, w in zip(ens.members, ws):
+            mem.set_fields(**w.fields)
+            mem.init_equilibrium()
+            mem.set_force(w.force_mode)
+        ens.set_option("persistent", persistent)
+        tuned = autotune.tune_ensemble(ens) if tune else {"lz": int(ens.get_option("lz"))}
+        ens.step(4)
+        ens.sync()
+        ens.profile(True, every=EVENT_STRIDE)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        ens.step(steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        prof = ens.profile_read()
+        ens.profile(False)
+        ens.sync()
+        ens.close()
+        return ms, tuned, prof
+
+    # the default mode (members' own steps on concurrent streams), then one
+    # persistent launch per step over all members (push form, CUDA graph)
+    ms, tuned, prof = timed(0)
+    persistent = 0
     value = sites * steps / (ms / 1e3) / 1e6
-    ens.close()
+    ms_p, tuned_p, prof_p = timed(1)
+    value_p = sites * steps / (ms_p / 1e3) / 1e6
     # the same members, one launch per member per step
     k_seq = min(steps, 40)
     solos = []
@@ -753,13 +763,21 @@ def measure_ensemble(n_members: int, steps: int, form: int, stream, tune: bool =
         d.close()
     peak, _ = measured_peak_gbs()
     achieved = BYTES_PER_SITE[form] * sites / (ms / steps / 1e3) / 1e9
+    achieved_p = BYTES_PER_SITE[form] * sites / (ms_p / steps / 1e3) / 1e9
     return {"workload": f"ensemble_{len(ws)}_members", "members": len(ws), "sites": sites,
             "member_sizes": sorted({w.shape[0] for w in ws}), "seed": 4, "steps": steps,
             "mlups": round(value, 3), "ms_per_step": round(ms / steps, 5),
             "sequential_mlups": round(seq, 3), "batched_over_sequential": round(value / seq, 3),
             "mode": "persistent launch + graph" if persistent else "members' one-launch steps on concurrent streams",
             "hbm_frac": round(achieved / peak, 4), "achieved_gbs": round(achieved, 1),
-            "tune": {k: v for k, v in tuned.items() if k != "timings"}, "gpu_launches": int(prof["launches"])}
+            "tune": {k: v for k, v in tuned.items() if k != "timings"}, "gpu_launches": int(prof["launches"]),
+            "persistent": {"mode": "one persistent launch per step over all members' tiles (push form, work items "
+                                   "taken from a counter), two steps per CUDA graph replay",
+                           "mlups": round(value_p, 3), "ms_per_step": round(ms_p / steps, 5),
+                           "hbm_frac": round(achieved_p / peak, 4), "achieved_gbs": round(achieved_p, 1),
+                           "batched_over_sequential": round(value_p / seq, 3),
+                           "tune": {k: v for k, v in tuned_p.items() if k != "timings"},
+                           "gpu_launches": int(prof_p["launches"])}}
 
 
 def run_ensemble(args):

@@ -213,6 +213,11 @@ bool push_tma_eligible(const dl_handle* h);
 bool push_eligible(const dl_handle* h);
 int push_step(dl_handle* h);
 int fast_settle(dl_handle* h);  // complete a push step's state (no-op when settled)
+// the persistent ensemble launch in the push form (step_push.cu)
+size_t push_args_bytes();
+void push_args_at(dl_handle* h, int k, void* out);
+int launch_push_batched(dl_handle* h0, const void* table, int nm, const int4* items, int nitems,
+                        const unsigned* nblk, unsigned* counter, int grid, cudaStream_t s);
 int fast_prepare_force(dl_handle* h, int mode);
 int spectral_project_f32(dl_handle* h, const float* d_u1, const float* d_u2, const float* d_u3);
 int spectral_adjoint_f32(dl_handle* h, const float* d_lf1, const float* d_lf2, const float* d_lf3, const float* d_u1,

@@ -1337,6 +1337,11 @@ struct BatchImpl {
     int graph_ok;
     int built_parity;       // member parity the tables were built at (-1: rebuild)
     int fmode, les;
+    int push;               // persistent mode in the push form (every member push-eligible)
+    int built_push;         // the form the tables were built for
+    unsigned char* h_ptable;  // push form: [2][nm] step arguments (host copy)
+    void* d_ptable;
+    unsigned* d_counter;    // push form: the launch's next work item
 };
 
 template <typename ST, bool RES, bool LES, int FMODE>
@@ -1376,6 +1381,11 @@ static int launch_batched_st(dl_handle* h0, BatchImpl* b, int k) {
 
 static int launch_batched(BatchImpl* b, int k) {
     dl_handle* h0 = b->mem[0];
+    if (b->push) {
+        const int grid = min(b->nitems, b->bps * b->sms);
+        return launch_push_batched(h0, (const unsigned char*)b->d_ptable + (size_t)k * b->nm * push_args_bytes(),
+                                   b->nm, b->d_items, b->nitems, b->d_nblk, b->d_counter, grid, b->stream);
+    }
     return b->form == DL_FORM_FP16 ? launch_batched_st<__half, true>(h0, b, k) : launch_batched_st<float, false>(h0, b, k);
 }
 
@@ -1424,7 +1434,10 @@ void batch_destroy(void* p) {
     cudaFree(b->d_nblk);
     cudaFree(b->d_pitems);
     cudaFree(b->d_pnblk);
+    cudaFree(b->d_ptable);
+    cudaFree(b->d_counter);
     free(b->h_table);
+    free(b->h_ptable);
     free(b);
 }
 
@@ -1471,12 +1484,23 @@ static int batch_build(BatchImpl* b) {
     for (int m = 0; m < nm; ++m) order[m] = m;
     for (int i = 1; i < nm; ++i)
         for (int j = i; j > 0 && b->mem[order[j]]->N > b->mem[order[j - 1]]->N; --j) std::swap(order[j], order[j - 1]);
+    const size_t psz = push_args_bytes();
+    if (b->push && !b->h_ptable) {
+        b->h_ptable = (unsigned char*)calloc(2 * (size_t)nm, psz);
+        if (!b->h_ptable) return set_error(h0, DL_ERR_ALLOC, "batch argument table");
+        DL_CUDA(h0, cudaMalloc(&b->d_ptable, 2 * (size_t)nm * psz));
+        DL_CUDA(h0, cudaMalloc(&b->d_counter, sizeof(unsigned)));
+    }
     for (int m = 0; m < nm; ++m) {
         dl_handle* h = b->mem[m];
         h->lz = min(b->lz, h->nz);
         for (int k = 0; k < 2; ++k) {
-            make_step_args(h, k, b->h_table[(size_t)k * nm + m]);
-            b->h_table[(size_t)k * nm + m].proj_in_step = 0;  // the batch projects in its own launch
+            if (b->push) {
+                push_args_at(h, k, b->h_ptable + ((size_t)k * nm + m) * psz);  // the projection is in the push body
+            } else {
+                make_step_args(h, k, b->h_table[(size_t)k * nm + m]);
+                b->h_table[(size_t)k * nm + m].proj_in_step = 0;  // the batch projects in its own launch
+            }
         }
         const int gx = (h->nx + TX - 1) / TX, gy = (h->ny + TY - 1) / TY, gz = (h->nz + h->lz - 1) / h->lz;
         nblk[m] = (unsigned)(gx * gy * gz);
@@ -1517,6 +1541,8 @@ static int batch_build(BatchImpl* b) {
     DL_CUDA(h0, cudaMemcpyAsync(b->d_nblk, nblk.data(), nm * sizeof(unsigned), cudaMemcpyHostToDevice, b->stream));
     DL_CUDA(h0, cudaMemcpyAsync(b->d_table, b->h_table, 2 * (size_t)nm * sizeof(FastArgs), cudaMemcpyHostToDevice,
                                 b->stream));
+    if (b->push)
+        DL_CUDA(h0, cudaMemcpyAsync(b->d_ptable, b->h_ptable, 2 * (size_t)nm * psz, cudaMemcpyHostToDevice, b->stream));
     DL_CUDA(h0, cudaStreamSynchronize(b->stream));
     if (b->graph_ok) {
         cudaGraphExecDestroy(b->gexec);
@@ -1545,6 +1571,7 @@ static int batch_build(BatchImpl* b) {
         b->graph_ok = 1;
     }
     b->built_parity = h0->cur;
+    b->built_push = b->push;
     return DL_OK;
 }
 
@@ -1613,17 +1640,40 @@ int batch_step(void* p, int nsteps) {
         if (h->P.walls && h->P.wall_start > h->step + 1 && h->P.wall_start <= h->step + nsteps)
             return set_error(h0, DL_ERR_UNSUPPORTED, "wall start inside a batched call; split the call");
     }
-    for (int m = 0; m < nm; ++m) {
-        int rc = fast_settle(b->mem[m]);  // the persistent launch steps the pull form
-        if (rc != DL_OK) return rc;
+    // the push form when every member takes it (FP32 members); else the pull form
+    bool push = true;
+    for (int m = 0; m < nm; ++m) push = push && push_eligible(b->mem[m]);
+    b->push = push ? 1 : 0;
+    int left = nsteps;
+    if (push) {
+        // the captured steps load a push step's (pending) state: members that
+        // are settled take one step of their own first, all of them, to stay in step
+        bool settled_any = false;
+        for (int m = 0; m < nm; ++m) settled_any = settled_any || !b->mem[m]->pushed;
+        if (settled_any && left > 0) {
+            for (int m = 0; m < nm; ++m) {
+                dl_handle* h = b->mem[m];
+                const cudaStream_t own = h->stream;
+                h->stream = h0->stream;  // ordered before the persistent launches
+                int rc = push_step(h);
+                h->stream = own;
+                if (rc != DL_OK) return rc;
+            }
+            left -= 1;
+        }
+    } else {
+        for (int m = 0; m < nm; ++m) {
+            int rc = fast_settle(b->mem[m]);  // the persistent launch steps the pull form
+            if (rc != DL_OK) return rc;
+        }
+        for (int m = 0; m < nm; ++m) {
+            const int dirty = b->mem[m]->fsp.dirty;
+            int rc = pre_step(b->mem[m]);
+            if (rc != DL_OK) return rc;
+            if (dirty) b->built_parity = -1;
+        }
     }
-    for (int m = 0; m < nm; ++m) {
-        const int dirty = b->mem[m]->fsp.dirty;
-        int rc = pre_step(b->mem[m]);
-        if (rc != DL_OK) return rc;
-        if (dirty) b->built_parity = -1;
-    }
-    if (b->built_parity < 0 || b->fmode != force_fmode(h0) || b->stream != h0->stream) {
+    if (b->built_parity < 0 || b->fmode != force_fmode(h0) || b->stream != h0->stream || b->built_push != b->push) {
         b->stream = h0->stream;
         int rc = batch_build(b);
         if (rc != DL_OK) return rc;
@@ -1632,7 +1682,15 @@ int batch_step(void* p, int nsteps) {
     // the step after it; the graph runs table 0 then table 1. (The tables'
     // absolute step numbers only feed the NaN report and the wall terms,
     // which are constant inside one call.)
-    int left = nsteps;
+    auto stepped = [&](int n) {
+        for (int m = 0; m < nm; ++m) {
+            advance(b->mem[m], n);
+            if (push) {
+                b->mem[m]->pushed = 1;
+                b->mem[m]->fsp.dirty = 0;
+            }
+        }
+    };
     while (left > 0) {
         const int k = (h0->cur == b->built_parity) ? 0 : 1;
         if (b->graph_ok && k == 0 && left >= 2) {
@@ -1640,14 +1698,14 @@ int batch_step(void* p, int nsteps) {
             DL_CUDA(h0, cudaGraphLaunch(b->gexec, b->stream));
             launch_end(h0, true);
             h0->launches += 1;  // the graph holds two step launches
-            for (int m = 0; m < nm; ++m) advance(b->mem[m], 2);
+            stepped(2);
             left -= 2;
         } else {
             launch_begin(h0);
             int rc = launch_batched(b, k);
             launch_end(h0, true);
             if (rc != DL_OK) return rc;
-            for (int m = 0; m < nm; ++m) advance(b->mem[m], 1);
+            stepped(1);
             left -= 1;
         }
     }

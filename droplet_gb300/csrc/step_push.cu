@@ -444,7 +444,7 @@ __device__ __forceinline__ void push_minmax(const FastArgs& a, float bmin, float
 // asynchronous copies, STG 1), or by one thread for the block (two tensor
 // copies completing on an mbarrier, STG 2; full tiles only)
 template <bool LES, int FMODE, bool SP, bool SETTLE, int STG = 0>
-__device__ __forceinline__ void push_body(const PushArgs& pa, float* smem) {
+__device__ __forceinline__ void push_body(const PushArgs& pa, float* smem, int bx, int by, int bz, unsigned nblk) {
     constexpr bool BULK = STG != 0;
     constexpr bool TMA = STG == 2;
     constexpr bool SPEC = FMODE == F_SPECTRAL;
@@ -472,9 +472,8 @@ __device__ __forceinline__ void push_body(const PushArgs& pa, float* smem) {
     const int nx = a.nx, ny = a.ny, nz = a.nz;
     const unsigned N = (unsigned)a.N;
     const unsigned nxy = (unsigned)nx * (unsigned)ny;
-    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
-    const int z0 = blockIdx.z * a.lz, z1 = min(z0 + a.lz, nz);
-    const unsigned nblk = gridDim.x * gridDim.y * gridDim.z;
+    const int x0 = bx * TX, y0 = by * TY;
+    const int z0 = bz * a.lz, z1 = min(z0 + a.lz, nz);
     const bool pend = pa.pending != 0;
     const bool fpend = SPEC && pend;  // band force to add at load
 
@@ -917,7 +916,7 @@ __device__ __forceinline__ void push_body(const PushArgs& pa, float* smem) {
     }
 
     if constexpr (SPEC) {
-        project_tile_sums(a, smem, s_tx1, s_ty1, cs, blockIdx.x + 3 * blockIdx.y + 5 * blockIdx.z);
+        project_tile_sums(a, smem, s_tx1, s_ty1, cs, bx + 3 * by + 5 * bz);
         spectral_block_done(a, smem, nblk);
     }
     if constexpr (SETTLE) {
@@ -937,19 +936,68 @@ __device__ __forceinline__ void push_body(const PushArgs& pa, float* smem) {
 template <bool LES, int FMODE, int STG>
 __global__ void __launch_bounds__(NT, 2) step_push(const __grid_constant__ PushArgs pa) {
     extern __shared__ __align__(128) float smem[];
-    push_body<LES, FMODE, false, false, STG>(pa, smem);
+    push_body<LES, FMODE, false, false, STG>(pa, smem, blockIdx.x, blockIdx.y, blockIdx.z,
+                                             gridDim.x * gridDim.y * gridDim.z);
 }
 
 template <int FMODE, int STG>
 __global__ void __launch_bounds__(NT, 2) step_push_sp(const __grid_constant__ PushArgs pa) {
     extern __shared__ __align__(128) float smem[];
-    push_body<false, FMODE, true, false, STG>(pa, smem);
+    push_body<false, FMODE, true, false, STG>(pa, smem, blockIdx.x, blockIdx.y, blockIdx.z,
+                                              gridDim.x * gridDim.y * gridDim.z);
+}
+
+// an ensemble's push steps as ONE persistent launch: work items (member, tile
+// x, tile y, z chunk), largest members first, taken one at a time from a
+// counter (zeroed before the launch) by whichever block is free, so that the
+// items' uneven lengths even out; each member's last block (of
+// nblk_of[member]) finalises its phi range and band coefficients. Up to
+// PUSH_CMAX members read their arguments from a constant-memory table (copied
+// there before each launch: the same access path as kernel parameters);
+// larger ensembles copy them into shared memory per work item.
+constexpr int PUSH_CMAX = 64;
+__constant__ PushArgs c_members[PUSH_CMAX];
+
+// the next work item of the block (uniform across it)
+__device__ __forceinline__ int next_item(unsigned* counter) {
+    __shared__ int s_w;
+    __syncthreads();  // the previous item's readers of s_w and of the rings are done
+    if (threadIdx.x == 0) s_w = (int)atomicAdd(counter, 1u);
+    __syncthreads();
+    return s_w;
+}
+
+template <bool LES, int FMODE>
+__global__ void __launch_bounds__(NT, 2) step_push_batched_c(const int4* __restrict__ items, int nitems,
+                                                             const unsigned* __restrict__ nblk_of,
+                                                             unsigned* counter) {
+    extern __shared__ __align__(128) float smem[];
+    for (int w = next_item(counter); w < nitems; w = next_item(counter)) {
+        const int4 it = items[w];
+        push_body<LES, FMODE, false, false, 0>(c_members[it.x], smem, it.y, it.z, it.w, nblk_of[it.x]);
+    }
+}
+
+template <bool LES, int FMODE>
+__global__ void __launch_bounds__(NT, 2) step_push_batched(const PushArgs* __restrict__ table,
+                                                           const int4* __restrict__ items, int nitems,
+                                                           const unsigned* __restrict__ nblk_of, unsigned* counter) {
+    extern __shared__ __align__(128) float smem[];
+    __shared__ PushArgs s_pa;
+    for (int w = next_item(counter); w < nitems; w = next_item(counter)) {
+        const int4 it = items[w];
+        const int* src = reinterpret_cast<const int*>(table + it.x);
+        int* dst = reinterpret_cast<int*>(&s_pa);
+        for (int t = threadIdx.x; t < (int)(sizeof(PushArgs) / sizeof(int)); t += blockDim.x) dst[t] = src[t];
+        __syncthreads();
+        push_body<LES, FMODE, false, false, 0>(s_pa, smem, it.y, it.z, it.w, nblk_of[it.x]);
+    }
 }
 
 template <int FMODE, bool SP>
 __global__ void __launch_bounds__(NT, 2) settle_push(const PushArgs pa) {
     extern __shared__ __align__(128) float smem[];
-    push_body<false, FMODE, SP, true>(pa, smem);
+    push_body<false, FMODE, SP, true>(pa, smem, blockIdx.x, blockIdx.y, blockIdx.z, gridDim.x * gridDim.y * gridDim.z);
 }
 
 // ---- host side ------------------------------------------------------------------
@@ -1113,6 +1161,67 @@ int push_step(dl_handle* h) {
     h->pushed = 1;
     h->fsp.dirty = 0;
     return DL_OK;
+}
+
+// ---- ensembles: the members' push steps as one persistent launch ----
+size_t push_args_bytes() { return sizeof(PushArgs); }
+
+// arguments of the push step k (0 or 1) steps after the handle's current
+// state, which must be a push step's (pending); for the tables a captured pair
+// of steps replays
+void push_args_at(dl_handle* h, int k, void* out) {
+    PushArgs pa;
+    memset(&pa, 0, sizeof(pa));
+    FastArgs& a = pa.a;
+    fill_fast(h, a);
+    const int c = h->cur ^ (k & 1), n = 1 - c;
+    a.f = h->fs[c];
+    a.g = h->gs[c];
+    a.fo = h->fs[n];
+    a.go = h->gs[n];
+    a.maco = nullptr;
+    a.mac = nullptr;
+    const int par = force_fmode(h) == F_SPECTRAL ? (h->fsp.par ^ (k & 1)) : h->fsp.par;
+    a.fh = h->fsp.d_fh[par];
+    a.fh_next = h->fsp.d_fh[1 - par];
+    a.step = h->step + 1 + k;
+    pa.pending = 1;
+    pa.walls_load = h->P.walls ? 1 : 0;
+    wall_terms(h, h->step + k, pa.wl_bot, pa.wl_top);
+    memcpy(out, &pa, sizeof(pa));
+}
+
+template <bool LES, int FMODE>
+static int launch_push_batched_t(dl_handle* h0, const void* table, int nm, const int4* items, int nitems,
+                                 const unsigned* nblk, unsigned* counter, int grid, cudaStream_t s) {
+    const size_t sm = sizeof(float) * (size_t)push_smem_floats(FMODE == F_SPECTRAL, false);
+    DL_CUDA(h0, cudaMemsetAsync(counter, 0, sizeof(unsigned), s));
+    if (nm <= PUSH_CMAX) {
+        static bool done[64] = {false};
+        int rc = configure_smem(h0, step_push_batched_c<LES, FMODE>, sm, done);
+        if (rc != DL_OK) return rc;
+        DL_CUDA(h0, cudaMemcpyToSymbolAsync(c_members, table, (size_t)nm * sizeof(PushArgs), 0,
+                                            cudaMemcpyDeviceToDevice, s));
+        step_push_batched_c<LES, FMODE><<<grid, NT, sm, s>>>(items, nitems, nblk, counter);
+    } else {
+        static bool done[64] = {false};
+        int rc = configure_smem(h0, step_push_batched<LES, FMODE>, sm, done);
+        if (rc != DL_OK) return rc;
+        step_push_batched<LES, FMODE><<<grid, NT, sm, s>>>(static_cast<const PushArgs*>(table), items, nitems, nblk,
+                                                           counter);
+    }
+    DL_CUDA(h0, cudaGetLastError());
+    return DL_OK;
+}
+
+int launch_push_batched(dl_handle* h0, const void* table, int nm, const int4* items, int nitems,
+                        const unsigned* nblk, unsigned* counter, int grid, cudaStream_t s) {
+    const int fmode = force_fmode(h0);
+#define DL_PB(L, F) launch_push_batched_t<L, F>(h0, table, nm, items, nitems, nblk, counter, grid, s)
+    if (h0->P.les)
+        return fmode == F_SPECTRAL ? DL_PB(true, F_SPECTRAL) : fmode == F_ARRAY ? DL_PB(true, F_ARRAY) : DL_PB(true, F_NONE);
+    return fmode == F_SPECTRAL ? DL_PB(false, F_SPECTRAL) : fmode == F_ARRAY ? DL_PB(false, F_ARRAY) : DL_PB(false, F_NONE);
+#undef DL_PB
 }
 
 int fast_settle(dl_handle* h) {

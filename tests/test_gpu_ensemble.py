@@ -1,8 +1,9 @@
 """Batched ensembles over members of uneven sizes and parameters, in both
 modes: the members' own steps launched concurrently (the default) and one
-persistent launch per step. Each member must get the result it gets when
-stepped on its own (bitwise without spectral forcing, whose FP64 accumulation
-order is not fixed; within FP32 rounding with it)."""
+persistent launch per step (in the push form when every member takes it, FP32;
+else the pull form). Each member must get the result it gets when stepped on
+its own in the same form (bitwise without spectral forcing, whose FP64
+accumulation order is not fixed; within FP32 rounding with it)."""
 import numpy as np
 import pytest
 
@@ -35,11 +36,11 @@ def start(sim, f, spectral):
     sim.set_force(_abi.DL_FORCE_SPECTRAL if spectral else _abi.DL_FORCE_NONE)
 
 
-@pytest.mark.parametrize("form", [FORM_FP32, FORM_FP16])
+@pytest.mark.parametrize("form,push", [(FORM_FP32, 1), (FORM_FP32, 0), (FORM_FP16, 0)])
 @pytest.mark.parametrize("persistent,spectral,les,graph,steps", [(1, False, False, 1, 7), (1, False, True, 0, 6),
                                                                  (1, True, True, 1, 9), (0, False, True, 0, 7),
                                                                  (0, True, True, 0, 9)])
-def test_ensemble_matches_members_stepped_alone(form, persistent, spectral, les, graph, steps):
+def test_ensemble_matches_members_stepped_alone(form, push, persistent, spectral, les, graph, steps):
     cases = [member_case(m, s, spectral, les) for m, s in enumerate(SHAPES)]
     ens = Ensemble([c[0] for c in cases], SHAPES, form)
     ens.set_option("persistent", persistent)
@@ -47,13 +48,15 @@ def test_ensemble_matches_members_stepped_alone(form, persistent, spectral, les,
     ens.set_option("graph", graph)
     ens.set_option("lz", 8)
     for mem, (P, f) in zip(ens.members, cases):
+        if form == FORM_FP32:
+            mem.set_option("push", push)
         start(mem, f, spectral)
     ens.step(steps)
     for m, (mem, (P, f)) in enumerate(zip(ens.members, cases)):
         solo = Droplet(P, SHAPES[m], form)
         solo.set_option("lz", 8)
-        if persistent and form == FORM_FP32:
-            solo.set_option("push", 0)  # the persistent launch steps the pull form
+        if form == FORM_FP32:
+            solo.set_option("push", push)
         start(solo, f, spectral)
         solo.step(steps)
         a, b = mem.get_fields(), solo.get_fields()
