@@ -126,6 +126,10 @@ __global__ void adj_walls(AdjArgs a) {
     block_add<1>(v, a.grads + 4 * (blockIdx.x % ADJ_NREP) + 3);
 }
 
+// PW: tau_g per site (LES and / or a viscosity ratio); LES: the Smagorinsky
+// term; SPEC: the band force. The plain step takes <false, false, false>, the
+// reverse of the initial equilibrium (no collision) too.
+template <bool PW, bool LES, bool SPEC>
 __global__ void __launch_bounds__(256) adj_local(AdjArgs a) {
     const long long s0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     const bool active = s0 < (long long)a.N;
@@ -160,8 +164,8 @@ __global__ void __launch_bounds__(256) adj_local(AdjArgs a) {
     const float dp0 = a.T / (omb * omb) - 2.f * a.a * phi;
     const float dA = (p0 - p0ref) - a.kf * phi * lap - a.kf6 * gsq;
     // per-site wg (LES and / or a viscosity ratio): G_ab = d u_a / d x_b, S, nu_t, nu(phi)
-    const bool les = a.les && a.stream;
-    const bool pw = (a.les || a.kvis != 0.f) && a.stream;
+    const bool les = LES && a.stream;
+    const bool pw = PW && a.stream;
     float G[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
     float tt = 0.f, wgs = a.omg, nut = 0.f;
     if (les) {
@@ -217,7 +221,7 @@ __global__ void __launch_bounds__(256) adj_local(AdjArgs a) {
             const float dfeq = HW(i) * dphi + FW(i) * dA + E * (3.f * phi * cu + a.kf * cGc);
             domf += ai * (dfeq - a.st[(size_t)i * N + s]);
         }
-        if (a.spec && a.stream) {
+        if (SPEC && a.stream) {
             lF[0] += 3.f * E * cx(i) * bi;
             lF[1] += 3.f * E * cy(i) * bi;
             lF[2] += 3.f * E * cz(i) * bi;
@@ -249,7 +253,7 @@ __global__ void __launch_bounds__(256) adj_local(AdjArgs a) {
     dkf += lA * (-phi * lap - gsq / 6.f);
     lphi += lA * (dp0 - a.kf * lap);
     const float lnu = pw ? lw * (-3.f * wgs * wgs * a.inv_ds) : 0.f;  // dL/dnu (and dL/dnu_t)
-    lphi += lnu * a.kvis;
+    if (PW) lphi += lnu * a.kvis;
     const float llap = -a.kf * phi * lA;
     lgsq -= a.kf6 * lA;
     lgr[0] += 2.f * gr[0] * lgsq;
@@ -265,7 +269,7 @@ __global__ void __launch_bounds__(256) adj_local(AdjArgs a) {
         a.aux[6 * N + s] = lu[0];
         a.aux[7 * N + s] = lu[1];
         a.aux[8 * N + s] = lu[2];
-        if (a.les) {
+        if (LES) {
             // dwg/dnu_t = -3 wg^2 / ds, dnu_t/dtt = csd / (2 sqrt(tt)), dtt/dG_ab = 4 S_ab
             const float ltt = (les && tt > 0.f) ? lnu * (0.5f * a.csd / sqrtf(tt)) : 0.f;
 #pragma unroll
@@ -274,8 +278,8 @@ __global__ void __launch_bounds__(256) adj_local(AdjArgs a) {
                 for (int be = 0; be < 3; ++be)
                     a.aux[(size_t)(9 + al + 3 * be) * N + s] = ltt * 2.f * (G[al][be] + G[be][al]);
         }
-        if (a.les || a.kvis != 0.f) a.aux[(size_t)18 * N + s] = wg;
-        if (a.spec) {
+        if (PW) a.aux[(size_t)18 * N + s] = wg;
+        if (SPEC) {
             a.aux[(size_t)19 * N + s] = lF[0];
             a.aux[(size_t)20 * N + s] = lF[1];
             a.aux[(size_t)21 * N + s] = lF[2];
@@ -290,6 +294,7 @@ __global__ void __launch_bounds__(256) adj_local(AdjArgs a) {
 // lphi(x) = lphi_loc(x) - 14 llap(x)/5 + sum_k [llap(x - c_k)/5 + c_k . lgrad(x - c_k)/10],
 // then the moments, plus the streamed (1 - w) part gathered from lin; writes
 // lout (and lphi into phi_out for the initial state)
+template <bool PW, bool LES>
 __global__ void __launch_bounds__(256) adj_stencil(AdjArgs a, float* phi_out) {
     const long long s0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (s0 >= (long long)a.N) return;
@@ -305,7 +310,7 @@ __global__ void __launch_bounds__(256) adj_stencil(AdjArgs a, float* phi_out) {
     const float lp = a.aux[5 * N + s] * (1.f / 3.f);
     float lu1 = a.aux[6 * N + s], lu2 = a.aux[7 * N + s], lu3 = a.aux[8 * N + s];
     float wg = a.stream ? a.omg : 1.f;
-    if (a.les && a.stream) {
+    if (LES && a.stream) {
         // transpose of G_ab(y) = inv_grad sum_k c_kb u_a(y + c_k): u_a(x) receives
         // inv_grad c_kb dL/dG_ab(x - c_k)
         float t[3] = {0.f, 0.f, 0.f};
@@ -325,7 +330,7 @@ __global__ void __launch_bounds__(256) adj_stencil(AdjArgs a, float* phi_out) {
         lu2 += a.inv_grad * t[1];
         lu3 += a.inv_grad * t[2];
     }
-    if ((a.les || a.kvis != 0.f) && a.stream) wg = a.aux[(size_t)18 * N + s];
+    if (PW && a.stream) wg = a.aux[(size_t)18 * N + s];
     if (phi_out) phi_out[s] = lphi;
     // the streamed part (1 - w) of the collision, gathered here rather than
     // stored by adj_local and read back
@@ -448,7 +453,15 @@ int adjoint_step(dl_handle* h, const float* d_state, long long step) {
             for (int k = 0; k < 5; ++k) w.wbot[k] = w.wtop[k] = 0.f;
         DL_LAUNCH(h, false, (adj_walls<<<nb(2 * plane), 256, 0, h->stream>>>(w)));
     }
-    DL_LAUNCH(h, true, (adj_local<<<nb(h->N), 256, 0, h->stream>>>(a)));
+    const bool pw = a.les || a.kvis != 0.f;
+    const unsigned g = nb(h->N);
+    cudaStream_t st = h->stream;
+    if (!pw && !a.spec) DL_LAUNCH(h, true, (adj_local<false, false, false><<<g, 256, 0, st>>>(a)));
+    else if (!pw) DL_LAUNCH(h, true, (adj_local<false, false, true><<<g, 256, 0, st>>>(a)));
+    else if (!a.les && !a.spec) DL_LAUNCH(h, true, (adj_local<true, false, false><<<g, 256, 0, st>>>(a)));
+    else if (!a.les) DL_LAUNCH(h, true, (adj_local<true, false, true><<<g, 256, 0, st>>>(a)));
+    else if (!a.spec) DL_LAUNCH(h, true, (adj_local<true, true, false><<<g, 256, 0, st>>>(a)));
+    else DL_LAUNCH(h, true, (adj_local<true, true, true><<<g, 256, 0, st>>>(a)));
     if (a.spec) {
         const size_t N = h->N;
         float* x = h->adj_aux;
@@ -457,7 +470,9 @@ int adjoint_step(dl_handle* h, const float* d_state, long long step) {
                                   x + 7 * N, x + 8 * N);
         if (rc != DL_OK) return rc;
     }
-    DL_LAUNCH(h, false, (adj_stencil<<<nb(h->N), 256, 0, h->stream>>>(a, nullptr)));
+    if (!pw) DL_LAUNCH(h, false, (adj_stencil<false, false><<<g, 256, 0, st>>>(a, nullptr)));
+    else if (!a.les) DL_LAUNCH(h, false, (adj_stencil<true, false><<<g, 256, 0, st>>>(a, nullptr)));
+    else DL_LAUNCH(h, false, (adj_stencil<true, true><<<g, 256, 0, st>>>(a, nullptr)));
     DL_CUDA(h, cudaGetLastError());
     h->adj_cur = 1 - h->adj_cur;
     return DL_OK;
@@ -473,8 +488,8 @@ int adjoint_init(dl_handle* h, const float* d_state0, float* d_lphi0) {
     a.lin = h->adj_lam[h->adj_cur];
     a.lout = h->adj_lam[1 - h->adj_cur];
     a.stream = 0;
-    DL_LAUNCH(h, false, (adj_local<<<nb(h->N), 256, 0, h->stream>>>(a)));
-    DL_LAUNCH(h, false, (adj_stencil<<<nb(h->N), 256, 0, h->stream>>>(a, d_lphi0)));
+    DL_LAUNCH(h, false, (adj_local<false, false, false><<<nb(h->N), 256, 0, h->stream>>>(a)));
+    DL_LAUNCH(h, false, (adj_stencil<false, false><<<nb(h->N), 256, 0, h->stream>>>(a, d_lphi0)));
     DL_CUDA(h, cudaGetLastError());
     h->adj_cur = 1 - h->adj_cur;
     return DL_OK;
