@@ -77,6 +77,19 @@ __device__ __forceinline__ constexpr float Ew(int i) { return i == 0 ? 2.0f / 9.
 __device__ __forceinline__ constexpr float Fw(int i) { return i == 0 ? -7.0f / 3.0f : (i <= 6 ? 1.0f / 3.0f : 1.0f / 24.0f); }
 __device__ __forceinline__ constexpr float c2w(int i) { return i == 0 ? 0.f : (i <= 6 ? 1.f : 3.f); }
 
+// x times a lattice constant c given exactly (in double) as the pair hi + lo of
+// floats: one rounding of the exact product, with no bias. A constant such as
+// 3 E_i = 1/3 rounded to one float is 3e-8 too large, the same at every site and
+// step; in the odd part of an equilibrium that scales sum_i c_i geq_i = u by
+// the same factor at every collision, and the error of u and of the phi flux
+// then grows linearly with the steps instead of as a random walk.
+__device__ __forceinline__ constexpr float c_hi(double c) { return (float)c; }
+__device__ __forceinline__ constexpr float c_lo(double c) { return (float)(c - (double)(float)c); }
+__device__ __forceinline__ float mulc(float x, double c) { return __fmaf_rn(x, c_hi(c), __fmul_rn(x, c_lo(c))); }
+// exact D3Q15 constants by class (0 rest, 1 axis, 2 diagonal)
+__device__ __forceinline__ constexpr double Ed(int c) { return c == 0 ? 2.0 / 9.0 : (c == 1 ? 1.0 / 9.0 : 1.0 / 72.0); }
+__device__ __forceinline__ constexpr double Fd(int c) { return c == 0 ? -7.0 / 3.0 : (c == 1 ? 1.0 / 3.0 : 1.0 / 24.0); }
+
 // c_i . (p, q, r) with the zero terms dropped; explicit roundings so that the
 // same inputs give the same bits wherever it is inlined
 __device__ __forceinline__ float cdot3(int i, float p, float q, float r) {
@@ -129,7 +142,9 @@ __device__ __forceinline__ float site_S(float dp, float u1, float u2, float u3) 
     return __fmaf_rn(-1.5f, usq, __fmul_rn(3.f, dp));
 }
 
-// local part of the equilibria (the FP16 residual basis), deviation form
+// local part of the equilibria (the FP16 residual basis), deviation form. (Its
+// constants stay single floats: the FP16 storage's own rounding dominates that
+// form's error, and the exact pairs cost it 5 % of its time.)
 __device__ __forceinline__ float fbar(int i, float dphi, float phi, float dp0, float cu) {
     if (i == 0) return __fmaf_rn(Fw(0), dp0, dphi);
     return __fmaf_rn(__fmul_rn(3.f * Ew(i), phi), cu, __fmul_rn(Fw(i), dp0));
@@ -276,8 +291,9 @@ __device__ __forceinline__ void collide_dir(const FastArgs& a, int i, const Rec&
     const float cGc = RES ? 4.5f * cg * cg - 1.5f * c2w(i) * r.gsq : (4.5f * cg) * cg - c2w(i) * r.gq;
     const float E = Ew(i);
     if (!RES) {
-        const float dfeq = (i == 0 ? r.dphi : 0.f) + Fw(i) * r.dA + E * (3.f * phi * cu + a.kf * cGc);
-        const float dgeq = E * (r.S + cu * (3.f + 4.5f * cu) + a.kg * cGc);
+        const float dfeq = (i == 0 ? r.dphi : 0.f) + mulc(r.dA, Fd(wclass(i))) +
+                           mulc(3.f * phi * cu + a.kf * cGc, Ed(wclass(i)));
+        const float dgeq = mulc(r.S + cu * (3.f + 4.5f * cu) + a.kg * cGc, Ed(wclass(i)));
         fo = fin + a.omf * (dfeq - fin);
         go = gin + r.omg * (dgeq - gin);
     } else {
@@ -299,7 +315,7 @@ __device__ __forceinline__ float collide_g(int i, float S, float omg, float u1, 
     const float E = Ew(i);
     float go;
     if (!RES) {
-        const float dgeq = E * (S + cu * (3.f + 4.5f * cu));
+        const float dgeq = mulc(S + cu * (3.f + 4.5f * cu), Ed(wclass(i)));
         go = gin + omg * (dgeq - gin);
     } else {
         go = gbar(i, S, cu) + gin + omg * (0.f - gin);

@@ -495,7 +495,7 @@ __device__ __forceinline__ void fused_body(const FastArgs& a, float* smem, int b
                 if (cz(i) == 1) u3n += go[i];
                 else if (cz(i) == -1) u3n -= go[i];
             }
-            dpn *= (1.0f / 3.0f);
+            dpn = mulc(dpn, 1.0 / 3.0);  // exact 1/3: no bias in p from step to step
             const unsigned d = zo[1] + yr[1] + xs[1];
             if (RES) {
                 const float phin = __fadd_rn(a.phi1, dphin);

@@ -325,8 +325,9 @@ __device__ __forceinline__ void collide_push(const PushArgs& pa, int t, const fl
     float* go = (float*)a.go;
     // destination index of direction i (x + c_i, wrapped)
     auto dst = [&](int i) -> unsigned { return (unsigned)i * N + zo[1 + cz(i)] + yr[1 + cy(i)] + xs[1 + cx(i)]; };
-    if (!SP) fo[dst(0)] = fmaf(wf, (dphi + Fw(0) * dA) - v[0], v[0]);
-    go[dst(0)] = fmaf(wg, Ew(0) * S - v[Q], v[Q]);
+    // (the lattice constants multiply as exact pairs, mulc: no bias from their rounding)
+    if (!SP) fo[dst(0)] = fmaf(wf, (dphi + mulc(dA, Fd(0))) - v[0], v[0]);
+    go[dst(0)] = fmaf(wg, mulc(S, Ed(0)) - v[Q], v[Q]);
     // per class (1 axis, 2 diagonal): even parts and odd coefficients of the equilibria
     float Kf[3] = {0.f, 0.f, 0.f}, Bf[3] = {0.f, 0.f, 0.f}, Af[3] = {0.f, 0.f, 0.f}, Kg[3], Ag[3];
 #pragma unroll
@@ -334,11 +335,11 @@ __device__ __forceinline__ void collide_push(const PushArgs& pa, int t, const fl
         const int i = c == 1 ? 1 : 7;
         const float E = Ew(i);
         if (!SP) {
-            Kf[c] = Fw(i) * dA - E * c2w(i) * a.kf * gq;
-            Bf[c] = (3.f * E) * phi;
-            Af[c] = (4.5f * E) * a.kf;
+            Kf[c] = mulc(dA, Fd(c)) - E * c2w(i) * a.kf * gq;
+            Bf[c] = mulc(phi, 3.0 * Ed(c));
+            Af[c] = (4.5f * E) * a.kf;  // 4.5 E_i = 1/2, 1/16: exact
         }
-        Kg[c] = E * (S - c2w(i) * a.kg * gq);
+        Kg[c] = mulc(S - c2w(i) * a.kg * gq, Ed(c));
         Ag[c] = 4.5f * E;
     }
     // c . v for the representatives 1, 2, 3 (axes) and 7, 8, 9, 10 (diagonals)
@@ -359,10 +360,10 @@ __device__ __forceinline__ void collide_push(const PushArgs& pa, int t, const fl
     // representative i (c_i) and its opposite j
     auto pairc = [&](int i, int j, int c) {
         const float cu = dotc(i, u1, u2, u3, uxy, uxmy);
-        const float e3 = 3.f * Ew(i);
-        const float gd = e3 * cu;  // odd part of geq
-        float fF = 0.f;            // the force term, odd
-        if (FMODE == F_ARRAY) fF = e3 * dotc(i, Fx, Fy, Fz, Fxy, Fxmy);
+        const double e3 = 3.0 * Ed(c);
+        const float gd = mulc(cu, e3);  // odd part of geq
+        float fF = 0.f;                 // the force term, odd
+        if (FMODE == F_ARRAY) fF = mulc(dotc(i, Fx, Fy, Fz, Fxy, Fxmy), e3);
         float ge;
         if (!SP) {
             const float cg = dotc(i, gx, gy, gz, gxy, gxmy);
@@ -620,7 +621,7 @@ __device__ __forceinline__ void push_body(const PushArgs& pa, float* smem, int b
         const float d1 = g[1] - g[4], d2 = g[2] - g[5], d3 = g[3] - g[6];
         const float d7 = g[7] - g[11], d8 = g[8] - g[12], d9 = g[9] - g[13], d10 = g[10] - g[14];
         pair_grad<float>(d1, d2, d3, d7, d8, d9, d10, u1, u2, u3);
-        dp = tsum<Q>(g) * (1.0f / 3.0f);
+        dp = mulc(tsum<Q>(g), 1.0 / 3.0);
     };
 
     // ---- staged planes (BULK) ----
