@@ -142,15 +142,16 @@ __device__ __forceinline__ float site_S(float dp, float u1, float u2, float u3) 
     return __fmaf_rn(-1.5f, usq, __fmul_rn(3.f, dp));
 }
 
-// local part of the equilibria (the FP16 residual basis), deviation form. (Its
-// constants stay single floats: the FP16 storage's own rounding dominates that
-// form's error, and the exact pairs cost it 5 % of its time.)
+// local part of the equilibria (the FP16 residual basis), deviation form; the
+// lattice constants multiply as exact pairs (mulc): the basis is part of every
+// post-collision value, so a biased constant would bias the fluxes (FP16 form,
+// config 2: phi~ error 1.1e-3 -> 2.8e-4 after 2000 steps, for 5 % of its time)
 __device__ __forceinline__ float fbar(int i, float dphi, float phi, float dp0, float cu) {
-    if (i == 0) return __fmaf_rn(Fw(0), dp0, dphi);
-    return __fmaf_rn(__fmul_rn(3.f * Ew(i), phi), cu, __fmul_rn(Fw(i), dp0));
+    if (i == 0) return __fadd_rn(dphi, mulc(dp0, Fd(0)));
+    return __fadd_rn(mulc(__fmul_rn(phi, cu), 3.0 * Ed(wclass(i))), mulc(dp0, Fd(wclass(i))));
 }
 __device__ __forceinline__ float gbar(int i, float S, float cu) {
-    return __fmul_rn(Ew(i), __fmaf_rn(cu, __fmaf_rn(4.5f, cu, 3.f), S));
+    return mulc(__fmaf_rn(cu, __fmaf_rn(4.5f, cu, 3.f), S), Ed(wclass(i)));
 }
 
 // ---- storage policies ----------------------------------------------------
@@ -299,9 +300,9 @@ __device__ __forceinline__ void collide_dir(const FastArgs& a, int i, const Rec&
     } else {
         const float fb = fbar(i, r.dphi, phi, r.dp0, cu);
         const float gb = gbar(i, r.S, cu);
-        const float df = Fw(i) * (r.dA - r.dp0) + E * a.kf * cGc;
+        const float df = mulc(r.dA - r.dp0, Fd(wclass(i))) + mulc(a.kf * cGc, Ed(wclass(i)));
         fo = fb + fin + a.omf * (df - fin);
-        go = gb + gin + r.omg * (E * a.kg * cGc - gin);
+        go = gb + gin + r.omg * (mulc(a.kg * cGc, Ed(wclass(i))) - gin);
     }
     if (FORCE && i != 0) go += 3.f * E * cdot3(i, r.Fx, r.Fy, r.Fz);
 }
