@@ -6,12 +6,15 @@ spectrum by shell (enesupe_cal, program/turbulence_hit_xy.f90:588-645) and the
 dissipation rate (program/turbulence_hit_xy.f90:426-463; both conventions
 differ by a constant factor, so one relative error covers them).
 
-Tolerances (checked at every 250 steps):
-  phi~ (= 2 (phi - phi1)/(phi2 - phi1) - 1) max error     <= 1e-3
-  |volume drift| (sum of w, relative)                     <= 2e-5
-  spectrum, L2 over shells, relative                      <= 1e-3
-  spectrum, worst shell holding >= 1e-3 of the peak       <= 1e-3
-  dissipation 2 nu <S:S>, relative                        <= 1e-3"""
+Tolerances (checked at every 250 steps), FP32 / FP16 storage:
+  phi~ (= 2 (phi - phi1)/(phi2 - phi1) - 1) max error     <= 5e-5 / 1e-3
+  |volume drift| (sum of w, relative)                     <= 2e-6 / 2e-5
+  spectrum, L2 over shells, relative                      <= 1e-5 / 1e-3
+  spectrum, worst shell holding >= 1e-3 of the peak       <= 2e-5 / 1e-3
+  dissipation 2 nu <S:S>, relative                        <= 1e-5 / 1e-3
+The FP32 bounds are ten times what the form reaches (phi~ 5.0e-6 after 1000
+steps); lattice weights rounded to single floats in the equilibria, whose
+bias is coherent from step to step, would exceed them (phi~ about 8e-4)."""
 import numpy as np
 import pytest
 
@@ -61,13 +64,15 @@ def curves():
     return out
 
 
+TOL = {FORM_FP32: {"phi_tilde": 5e-5, "volume": 2e-6, "spec_l2": 1e-5, "spec_max": 2e-5, "diss": 1e-5},
+       FORM_FP16: {"phi_tilde": 1e-3, "volume": 2e-5, "spec_l2": 1e-3, "spec_max": 1e-3, "diss": 1e-3}}
+
+
 @pytest.mark.parametrize("form", [FORM_FP32, FORM_FP16])
 def test_long_horizon_errors_against_fp64(curves, form):
+    tol = TOL[form]
     for k, row in enumerate(curves[form]):
         step = (k + 1) * EVERY
         print(form, step, row)
-        assert row["phi_tilde"] <= 1e-3, (step, row)
-        assert abs(row["volume"]) <= 2e-5, (step, row)
-        assert row["spec_l2"] <= 1e-3, (step, row)
-        assert row["spec_max"] <= 1e-3, (step, row)
-        assert abs(row["diss"]) <= 1e-3, (step, row)
+        for key, bound in tol.items():
+            assert abs(row[key]) <= bound, (step, key, row)
