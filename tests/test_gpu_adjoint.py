@@ -266,3 +266,42 @@ def test_adjoint_viscosity_ratio_matches_fp64_finite_differences(adjoint_visc):
         h = 1e-4 * abs(base)
         fd = (fp64_loss(mk(h), w, VISC_STEPS) - fp64_loss(mk(-h), w, VISC_STEPS)) / (2 * h)
         assert abs(g[name] - fd) <= 2e-2 * abs(fd) + 1e-12, (name, g[name], fd)
+
+
+@pytest.mark.parametrize("push", [0, 1])
+def test_reloaded_state_continues_the_forced_run(push):
+    """dl_save_state / dl_load_state in the middle of a run with the band force:
+    the reloaded state takes its next band coefficients from its own u, so the
+    continued run ends where the uninterrupted one does (within FP32 rounding:
+    the coefficients are projected once by a separate launch instead of inside
+    the step), and far from where stale coefficients would take it."""
+    import ctypes as C
+
+    w = configs.forced_turbulence(n=32, radius=6.0, urms=0.01, taug=0.6, eps=1e-5, steps=30, form=32)
+
+    def make():
+        d = Droplet(w.params, w.shape, 32)
+        d.set_option("push", push)
+        d.set_fields(**w.fields)
+        d.init_equilibrium()
+        d.set_force(_abi.DL_FORCE_SPECTRAL)
+        return d
+
+    a = make()
+    a.step(30)
+    ref = a.get_fields()
+    b = make()
+    n = C.c_int64()
+    b._lib.dl_state_floats(b._h, C.byref(n))
+    buf = torch.empty(int(n.value), dtype=torch.float32, device="cuda")
+    b.step(10)
+    b._call("save_state", C.c_void_p(buf.data_ptr()))
+    b.step(10)  # moves the band coefficients on
+    b._call("load_state", C.c_void_p(buf.data_ptr()))
+    b.step_count = 10
+    b.step(20)
+    got = b.get_fields()
+    for k in ("phi", "u1", "u2", "u3"):
+        assert np.abs(got[k] - ref[k]).max() <= 1e-6 * max(1.0, np.abs(ref[k]).max()), k
+    a.close()
+    b.close()
