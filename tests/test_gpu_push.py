@@ -234,3 +234,22 @@ def test_tensor_stage_wait_limit_reports_timeout():
     h.step(3)
     h.sync()
     assert np.isfinite(h.get_fields()["phi"]).all()
+
+
+@pytest.mark.parametrize("lz", [1, 5])
+def test_tensor_staged_planes_with_uneven_z_chunks(lz):
+    """Stage 2 (tensor copies) with z chunks that do not divide nz (5, 5, 4 of
+    14) and with chunks of a single plane: the same bits as loads into registers."""
+    shape = (64, 16, 14)
+    P, f, mode, force = make_case("les_static_force", shape)
+    out = {}
+    for stage in (0, 2):
+        g = Droplet(P, shape, FORM_FP32)
+        g.set_option("stage", stage)
+        g.set_option("lz", lz)
+        start(g, f, mode, force)
+        g.step(7)
+        out[stage] = g.get_fields()
+        g.sync()
+    for k in out[0]:
+        assert np.array_equal(out[0][k], out[2][k]), k
