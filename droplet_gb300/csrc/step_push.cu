@@ -119,6 +119,9 @@ struct PushArgs {
 
 // staged populations of the next plane, one column per thread: [2 Q][NT]
 constexpr int PB_FLOATS = 2 * Q * NT;
+// floats of the staged plane: f and g, or (single phase) g only, at this offset
+__host__ __device__ constexpr int pb_floats(bool sp) { return sp ? Q * NT : PB_FLOATS; }
+__host__ __device__ constexpr int pb_goff(bool sp) { return sp ? 0 : Q * NT; }
 
 // shared-memory footprint in floats
 // (rings and tables, then, stage 1 or 2, the staged plane at a 128-byte
@@ -132,7 +135,7 @@ __host__ __device__ constexpr int push_rings_floats(bool spec, bool sp) {
 }
 __host__ __device__ constexpr int push_stage_offset(bool spec, bool sp) { return (push_rings_floats(spec, sp) + 31) / 32 * 32; }
 __host__ __device__ constexpr int push_smem_floats(bool spec, bool sp, int stage = 0) {
-    return stage == 0 ? push_rings_floats(spec, sp) : push_stage_offset(spec, sp) + PB_FLOATS + (stage == 2 ? 36 : 0);
+    return stage == 0 ? push_rings_floats(spec, sp) : push_stage_offset(spec, sp) + pb_floats(sp) + (stage == 2 ? 36 : 0);
 }
 static_assert(PSL * P1 * 4 + PSL * P2 * FENT >= PT_SCRATCH, "projection scratch exceeds the rings");
 
@@ -461,12 +464,13 @@ __device__ __forceinline__ void push_body(const PushArgs& pa, float* smem, int b
     float2* s_ty2 = s_tx2 + SNK * EX2;                             // [SNK][EY2] e^{i ky y}, y = y0-2+ey
     float2* s_tx1 = s_ty2 + SNK * EY2;                             // [SNK][EX1] projection tables
     float2* s_ty1 = s_tx1 + SNK * EX1;                             // [SNK][EY1]
-    float* s_pb = smem + push_stage_offset(SPEC, SP);                  // [2 Q][NT] staged plane (BULK)
+    float* s_pb = smem + push_stage_offset(SPEC, SP);  // staged plane (BULK): [2 Q][NT], single phase [Q][NT]
     if (TMA) {  // at a 128-byte boundary of the shared window (the room is in the footprint)
         const unsigned off = (unsigned)__cvta_generic_to_shared(s_pb);
         s_pb += ((128u - (off & 127u)) & 127u) / 4u;
     }
-    unsigned long long* s_bar = reinterpret_cast<unsigned long long*>(s_pb + PB_FLOATS);  // (TMA)
+    unsigned long long* s_bar = reinterpret_cast<unsigned long long*>(s_pb + pb_floats(SP));  // (TMA)
+    float* s_pg = s_pb + pb_goff(SP);  // the staged g
 
     const int tid = threadIdx.x;
     const int tx = tid % TX, ty = tid / TX;
@@ -640,7 +644,7 @@ __device__ __forceinline__ void push_body(const PushArgs& pa, float* smem, int b
                 const int zw = wrap_near(zp, nz);
                 mbar_expect_tx(s_bar, (SP ? 1u : 2u) * Q * NT * (unsigned)sizeof(float) + pa.extra_tx);
                 if (!SP) tma_load_plane(s_pb, &pa.tmf, s_bar, x0, y0, zw);
-                tma_load_plane(s_pb + Q * NT, &pa.tmg, s_bar, x0, y0, zw);
+                tma_load_plane(s_pg, &pa.tmg, s_bar, x0, y0, zw);
             }
             return;
         }
@@ -650,7 +654,7 @@ __device__ __forceinline__ void push_body(const PushArgs& pa, float* smem, int b
             for (int i = 0; i < Q; ++i) cp_async4(s_pb + i * NT + tid, (const float*)a.f + (unsigned)i * N + s);
         }
 #pragma unroll
-        for (int i = 0; i < Q; ++i) cp_async4(s_pb + (Q + i) * NT + tid, (const float*)a.g + (unsigned)i * N + s);
+        for (int i = 0; i < Q; ++i) cp_async4(s_pg + i * NT + tid, (const float*)a.g + (unsigned)i * N + s);
         cp_async_commit();
     };
     auto bulk_take = [&](float* v) {
@@ -669,7 +673,7 @@ __device__ __forceinline__ void push_body(const PushArgs& pa, float* smem, int b
             for (int i = 0; i < Q; ++i) v[i] = s_pb[i * NT + tid];
         }
 #pragma unroll
-        for (int i = 0; i < Q; ++i) v[Q + i] = s_pb[(Q + i) * NT + tid];
+        for (int i = 0; i < Q; ++i) v[Q + i] = s_pg[i * NT + tid];
     };
 
     // ---- prologue: band force tables and planes ----
