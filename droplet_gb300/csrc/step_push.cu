@@ -63,6 +63,14 @@ __device__ __forceinline__ void cp_async4(float* smem_dst, const float* gmem_src
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
+// a population of the loaded state: read once per step, so it takes no L1 line
+// (L1 stays for the kernel's register spill, which it would otherwise evict)
+__device__ __forceinline__ float ld_stream(const float* p) {
+    float v;
+    asm("ld.global.nc.L1::no_allocate.f32 %0, [%1];" : "=f"(v) : "l"(p));
+    return v;
+}
+
 // ---- tensor copies (TMA) completing on an mbarrier ----
 __device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
     const unsigned b = (unsigned)__cvta_generic_to_shared(bar);
@@ -576,11 +584,11 @@ __device__ __forceinline__ void push_body(const PushArgs& pa, float* smem, int b
         const unsigned s = (unsigned)wrap_near(zp, nz) * nxy + c;
         if (withf) {
 #pragma unroll
-            for (int i = 0; i < Q; ++i) v[i] = __ldg((const float*)a.f + (unsigned)i * N + s);
+            for (int i = 0; i < Q; ++i) v[i] = ld_stream((const float*)a.f + (unsigned)i * N + s);
         }
         if (withg) {
 #pragma unroll
-            for (int i = 0; i < Q; ++i) v[Q + i] = __ldg((const float*)a.g + (unsigned)i * N + s);
+            for (int i = 0; i < Q; ++i) v[Q + i] = ld_stream((const float*)a.g + (unsigned)i * N + s);
         }
     };
     // the pending part of the loaded g of the site at ring position (ex, ey) of plane zp:
