@@ -378,7 +378,7 @@ def cpu_protocol_env():
 
 E2E_MIN_STEPS = 1000  # steps of the end-to-end run (at least; more when --steps is larger)
 OUTPUT_EVERY = 1000   # field output interval of the end-to-end run
-CPU_WARMUP, CPU_REPS, CPU_STEPS = 20, 5, 200  # BASELINE protocol: 20 warm-up + 5 x 200 timed steps, median
+CPU_WARMUP, CPU_REPS, CPU_STEPS = 20, 5, 200  # CPU timing protocol: 20 warm-up + 5 x 200 timed steps, median
 
 
 def cpu_protocol(w, budget_s: float, warmup: int = CPU_WARMUP, reps: int = CPU_REPS, steps: int = CPU_STEPS):
